@@ -1,0 +1,346 @@
+"""Capon/MVDR throughput benchmark (one JSON line on stdout).
+
+Workload: Xd [Nx=256][Ny=2048][M=64] complex64 (synthetic, 8 scatterers at
+20 dB per element), L=32, K=2 (5 range samples), loading 0.01*tr(R)/L,
+a = ones(32): 256 x 2044 = 523,264 pixels per step.  Outputs per pixel:
+complex amplitude z and power P.
+
+  value   pixels/s of the fused kernel with the cube resident in HBM
+          (one launch per step; the 268 MB cube exceeds the 126 MB L2, so
+          every step streams it from HBM)
+  e2e     pixels/s through cos_capon_get_capon_ex with pinned host buffers:
+          H2D of the cube, the launch and D2H of z and P inside each step
+  plain   pixels/s of the plain FP32 three-stage form (the denominator of the
+          metric), same workload
+
+``--impl reference`` times the reference's own CPU Capon path
+(getCaponC.getCaponCPy, compiled from the reference sources into oracle/_ref)
+on all host cores, or the FP64 C oracle when that module is not built.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+M, L, K, NX, NY, D = 64, 32, 2, 256, 2048, 0.01
+NS, T = M - L + 1, 2 * K + 1
+NPIX = NX * (NY - 2 * K)
+# Algorithmic work per pixel (canonical count: full-array Gram covariance with
+# diagonal smoothing 8 M^2 T + 2 L^2 Ns, Cholesky 4/3 L^3, two triangular
+# solves 8 L^2, weights/outputs 32 L + 8 M).
+FLOP_PER_PIXEL = 8 * M * M * T + 2 * L * L * NS + (4.0 / 3.0) * L ** 3 + 8 * L * L + 32 * L + 8 * M
+# Floating-point work the fused kernel actually executes per pixel (useful
+# operations, complex MAC = 8 flop): covariance rows 1..L-1 by the diagonal
+# recurrence (2T MACs per upper-triangle entry), row 0 and subarray sums
+# amortised per range row, Cholesky, two forward solves, outputs.
+EXEC_FLOP_PER_PIXEL = (8 * 2 * T * (L * (L + 1) // 2 - L) + 8 * NS * L + 2 * NS * L + 2 * T * L
+                       + (4.0 / 3.0) * L ** 3 + 2 * 8 * L * L / 2 * 2 + 16 * L)
+# Algorithmic HBM bytes per pixel: the cube once (8 M Ny/(Ny-2K)) + z + P.
+BYTES_PER_PIXEL = 8 * M * NY / (NY - 2 * K) + 8 + 4
+CONFIG = {"workload": "capon-element-space M=64 L=32 K=2 [Nx=256,Ny=2048]", "M": M, "L": L, "K": K,
+          "Nx": NX, "Ny": NY, "pixels_per_step": NPIX, "loading": D, "outputs": "z,P",
+          "l2": "inputs larger than L2 (268 MB cube vs 126 MB L2)", "parallelism": "replicas"}
+
+
+def _peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return {}
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, dev: int):
+        self.dev, self.proc, self.out = dev, None, []
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.out.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+            self.t.join(timeout=2)
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.out:
+            f = [v.strip() for v in line.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def fp32_peak_tflops(torch) -> float:
+    """cuBLAS FP32 SGEMM throughput (TF32 off): the measured CUDA-core FP32 peak."""
+    torch.backends.cuda.matmul.allow_tf32 = False
+    n = 8192
+    a = torch.randn(n, n, device="cuda")
+    b = torch.randn(n, n, device="cuda")
+    for _ in range(2):
+        torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 0.0
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        e1.synchronize()
+        best = max(best, 2 * n ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    del a, b
+    return best
+
+
+def cpu_reference_rate(cores: int, beams: int, seed: int = 1) -> dict:
+    """Reference CPU Capon on `beams` beams of the workload, all `cores`
+    processes; returns pixels/s and what ran."""
+    from cos_gb300 import synth
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ref  # noqa: E402
+    x = synth.cube(NY, beams, M, [10.0] * 8, seed)
+    if ref.available():
+        import multiprocessing as mp
+        ctx = mp.get_context("spawn")
+        slabs = np.array_split(np.arange(beams), cores)
+        slabs = [s for s in slabs if len(s)]
+        with ctx.Pool(len(slabs), initializer=_ref_init) as pool:
+            pool.map(_ref_slab, [np.ascontiguousarray(x[s[:1], :64]) for s in slabs])   # warm-up
+            t0 = time.perf_counter()
+            pool.map(_ref_slab, [np.ascontiguousarray(x[s]) for s in slabs])
+            dt = time.perf_counter() - t0
+        kind = "reference"
+        what = "getCaponC.getCaponCPy (reference Cython, FP64) in a spawn pool"
+    else:
+        import oracle  # noqa: E402
+        oracle.capon(x[:1, :64], D, L, K, nthreads=1)
+        t0 = time.perf_counter()
+        oracle.capon(x, D, L, K, nthreads=cores)
+        dt = time.perf_counter() - t0
+        kind = "port"
+        what = "FP64 C restatement (oracle/capon_oracle.c), pthreads"
+    npx = beams * (NY - 2 * K)
+    return {"value": npx / dt, "unit": "pixels/s", "cores": cores, "kind": kind,
+            "sample": f"{beams} beams x {NY - 2 * K} pixels of the workload ({npx} pixels), {what}",
+            "seconds": dt}
+
+
+def _ref_init():
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ref  # noqa: E402
+    global _REF
+    _REF = ref.load()
+
+
+def _ref_slab(x):
+    _REF.getCaponCPy(x.astype(np.complex128), D, L, K, np.array([]), False, False)
+    return 0
+
+
+def run_reference(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    beams = max(cores, 8)
+    vals = []
+    last = None
+    for i in range(args.warmup + args.steps):
+        r = cpu_reference_rate(cores, beams, seed=1 + i)
+        if i >= args.warmup:
+            vals.append(r["value"])
+        last = r
+    v = statistics.median(vals)
+    npx_step = beams * (NY - 2 * K)
+    line = {"metric": METRIC, "value": v, "unit": "pixels/s", "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": npx_step / v * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+            "data": "synthetic", "config": CONFIG,
+            "cpu_baseline": {k: last[k] for k in ("unit", "cores", "kind", "sample")} | {"value": v},
+            "e2e": {"value": v, "unit": "pixels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+METRIC = "Capon pixels/s at L=32 (fast vs plain FP32 GPU; <=1e-4 rel err vs FP64)"
+
+
+def run_gpu(args) -> None:
+    import torch
+    from cos_gb300 import _lib, capon, synth
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    x_host = synth.config1(seed=1 + rank)["x"]
+    xt = torch.from_numpy(x_host).cuda()
+    npy = NY - 2 * K
+    ctx = capon.Context()
+    stream = torch.cuda.Stream()
+
+    def frame(form_P=True):
+        f = capon.DeviceFrame(x=xt, L=L, K=K, d=D,
+                              z=torch.empty((NX, npy), dtype=torch.complex64, device="cuda"),
+                              P=torch.empty((NX, npy), dtype=torch.float32, device="cuda"))
+        return f
+
+    def time_form(form: int, steps: int, warmup: int):
+        f = frame()
+        o = capon.opts(form=form)
+        with torch.cuda.stream(stream):
+            for _ in range(warmup):
+                capon.capon_frames([f], ctx, o, stream)
+        stream.synchronize()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            for _ in range(steps):
+                capon.capon_frames([f], ctx, o, stream)
+            e1.record(stream)
+        e1.synchronize()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        if dist:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, f
+
+    # fused (headline), with clocks sampled during the timed region
+    with Clocks(local) as clk:
+        ms, f = time_form(_lib.FORM_FUSED, args.steps, args.warmup)
+    clocks = clk.summary()
+    value = NPIX * world / (ms * 1e-3)
+
+    # plain FP32 three-stage form (denominator), fewer steps
+    ms_plain, _ = time_form(_lib.FORM_PLAIN, max(2, min(args.steps, 5)), max(1, min(args.warmup, 2)))
+
+    # e2e through the host-pointer C-ABI call, pinned host buffers
+    xp = torch.from_numpy(x_host).pin_memory()
+    zp = torch.empty((NX, npy), dtype=torch.complex64).pin_memory()
+    Pp = torch.empty((NX, npy), dtype=torch.float32).pin_memory()
+    cctx = capon.Capon()
+    xn, zn, Pn = xp.numpy(), zp.numpy(), Pp.numpy()
+    for _ in range(max(1, args.warmup)):
+        _lib.check(cctx.getCaponEx(zn, Pn, None, None, xn, D, L, K, M, NX, NY, 0))
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        _lib.check(cctx.getCaponEx(zn, Pn, None, None, xn, D, L, K, M, NX, NY, 0))
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    if dist:
+        t = torch.tensor([e2e_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+
+    # parity of this very run against the FP64 oracle on sampled beams
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle  # noqa: E402
+    beams = [0, 128, 255]
+    refo = oracle.capon(np.ascontiguousarray(x_host[beams]), D, L, K, want_w=False, nthreads=3)
+    Pg = f.P.cpu().numpy()[beams]
+    relP = np.abs(Pg - refo["P"]) / refo["P"]
+
+    peaks = _peaks()
+    fp32 = fp32_peak_tflops(torch)
+    hbm_peak = peaks.get("hbm_gbs")
+    kernel_s = ms * 1e-3
+    achieved_tf = FLOP_PER_PIXEL * NPIX / kernel_s / 1e12
+    exec_tf = EXEC_FLOP_PER_PIXEL * NPIX / kernel_s / 1e12
+    achieved_gbs = BYTES_PER_PIXEL * NPIX / kernel_s / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": "pixels/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator, 8 scatterers, 20 dB)",
+        "config": CONFIG,
+        "plain": {"value": NPIX * world / (ms_plain * 1e-3), "ms_per_step": ms_plain,
+                  "speedup_fused_over_plain": ms_plain / ms},
+        "parity": {"P_rel_err_max": float(relP.max()), "P_rel_err_median": float(np.median(relP)),
+                   "sample": "beams 0,128,255 vs FP64 oracle"},
+        "e2e": {"value": NPIX * world / (e2e_ms * 1e-3), "unit": "pixels/s", "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": int(x_host.nbytes), "d2h_bytes_per_step": int(zn.nbytes + Pn.nbytes)},
+        "gpu_launches": args.steps,
+        "roofline": {"bound": "fp32", "achieved": achieved_tf, "peak": fp32, "unit": "TFLOP/s",
+                     "frac": achieved_tf / fp32, "traffic": None,
+                     "peak_source": "measured here: cuBLAS FP32 SGEMM 8192^3, TF32 off",
+                     "flop_per_pixel": FLOP_PER_PIXEL,
+                     "executed_flop_per_pixel": EXEC_FLOP_PER_PIXEL, "executed_tflops": exec_tf,
+                     "executed_frac": exec_tf / fp32},
+        "roofline_hbm": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": (achieved_gbs / hbm_peak) if hbm_peak else None,
+                         "bytes_per_pixel": BYTES_PER_PIXEL, "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = {k: v for k, v in cpu_reference_rate(os.cpu_count() or 1, 16).items()
+                                if k != "seconds"}
+    if rank == 0:
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,413 @@
+// Host side of the C ABI declared in include/cos_capon.h.
+//
+// The context plays the role of the reference's Capon object
+// (RealTimeCapon/Capon.h:13-125): it caches device buffers that grow on demand
+// (Capon.cpp:110-148, 465-547) and returns CUDA error numbers as status.
+// Unlike the reference it runs every stage on one stream without host
+// synchronisation between stages, and keeps covariance matrices on chip.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <new>
+#include <vector>
+
+#include "capon_internal.h"
+#include "../../include/cos_capon.h"
+
+using namespace cgb;
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    int ensure(size_t bytes)
+    {
+        if (bytes <= cap) return 0;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        if (cudaMalloc(&p, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            return COS_CAPON_ERR_OUT_OF_MEMORY;
+        }
+        cap = bytes;
+        return 0;
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+struct cos_capon_ctx {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    unsigned *d_status = nullptr;
+    // host-pointer call buffers
+    DevBuf x, z, P, w, R;
+    // plain-pipeline scratch
+    DevBuf Rwork, Ria;
+    // stage entry points
+    DevBuf A, b, sol;
+};
+
+static const cos_capon_opts kDefaultOpts = {COS_CAPON_FORM_FUSED, COS_CAPON_LOAD_ELEMENT, COS_CAPON_R_REFERENCE, 0};
+
+// Argument checks of Capon::getCapon (Capon.cpp:98-107) and BuildR::getR
+// (BuildR.cpp:37-48), plus this build's own limits.
+static int check_sizes(int L, int K, int M, int Nx, int Ny, int Nb)
+{
+    if (Nx < 1 || Ny < 1 || L < 1 || M < 1 || K < 0 || Nb < 0) return COS_CAPON_ERR_LAUNCH;
+    if (Nb > L) return COS_CAPON_ERR_LAUNCH;
+    if (L > M) return COS_CAPON_ERR_LAUNCH;
+    if (2 * K >= Ny) return COS_CAPON_ERR_LAUNCH;
+    if (L > 64) return COS_CAPON_ERR_NOT_SUPPORTED;
+    return 0;
+}
+
+// Reference behaviour: refuse a problem that does not fit in free device memory
+// (largerThanMaxSupportedSize, Capon.cpp:549-567).
+static int check_free(size_t need)
+{
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
+        cudaGetLastError();
+        return COS_CAPON_ERR_OUT_OF_MEMORY;
+    }
+    return need > fr ? COS_CAPON_ERR_OUT_OF_MEMORY : 0;
+}
+
+static FrameDev make_frame(const cos_capon_frame &fr, const cos_capon_opts &o)
+{
+    FrameDev f;
+    memset(&f, 0, sizeof(f));
+    f.x = (const float2 *)fr.x;
+    f.z = (float2 *)fr.z;
+    f.P = fr.P;
+    f.w = (float2 *)fr.w;
+    f.R = (float2 *)fr.R;
+    f.d = fr.d;
+    f.L = fr.L;
+    f.K = fr.K;
+    f.M = fr.M;
+    f.Nx = fr.Nx;
+    f.Ny = fr.Ny;
+    f.Nb = fr.Nb;
+    f.Npy = fr.Ny - 2 * fr.K;
+    f.loading = o.loading;
+    f.r_layout = o.r_layout;
+    f.refine = o.refine;
+    return f;
+}
+
+static bool use_fused(const FrameDev &f, const cos_capon_opts &o)
+{
+    return o.form == COS_CAPON_FORM_FUSED && f.Nb == 0 && fused_supported(f.L) && 2 * f.K + 1 <= fused_tmax(f.L);
+}
+
+// plain three-stage pipeline for one element-space frame
+static int run_plain(cos_capon_ctx *c, FrameDev f, cudaStream_t s)
+{
+    const size_t npix = (size_t)f.Nx * f.Npy;
+    int e = c->Rwork.ensure(npix * f.L * f.L * sizeof(float2));
+    if (e) return e;
+    if ((e = c->Ria.ensure(npix * f.L * sizeof(float2)))) return e;
+    float2 *Rw = (float2 *)c->Rwork.p, *Ria = (float2 *)c->Ria.p;
+    if ((e = launch_plain_build_r(f, Rw, 1, s))) return e;
+    if ((e = launch_plain_solve_hpd(f, Rw, Ria, c->d_status, s))) return e;
+    if ((e = launch_plain_output(f, Ria, s))) return e;
+    if (f.R) {
+        // the requested R layout, written by a second covariance pass
+        e = launch_plain_build_r(f, f.R, f.r_layout == COS_CAPON_R_REFERENCE ? 1 : 0, s);
+    }
+    return e;
+}
+
+static int run_frames(cos_capon_ctx *c, const FrameDev *fs, int n, const cos_capon_opts &o, cudaStream_t s)
+{
+    // batch consecutive fused frames with equal (L, K, M) into one launch
+    int i = 0;
+    while (i < n) {
+        const FrameDev &f = fs[i];
+        if (use_fused(f, o)) {
+            FramesParam fp;
+            memset(&fp, 0, sizeof(fp));
+            long long begin = 0;
+            int j = i;
+            while (j < n && fp.n < kMaxFrames && use_fused(fs[j], o) && fs[j].L == f.L && fs[j].K == f.K &&
+                   fs[j].M == f.M) {
+                FrameDev g = fs[j];
+                g.tile = fused_tile(g.L);
+                g.tiles_per_beam = (g.Npy + g.tile - 1) / g.tile;
+                g.tile_begin = begin;
+                begin += (long long)g.Nx * g.tiles_per_beam;
+                fp.f[fp.n++] = g;
+                ++j;
+            }
+            int e = launch_fused_frames(fp, c->d_status, c->num_sms, s);
+            if (e) return e;
+            i = j;
+        } else if (f.Nb > 0) {
+            int e = launch_beamspace(f, nullptr, s);
+            if (e) return e;
+            if (f.R) {  // element-space loaded R, as the reference copies it back (Capon.cpp:253-259)
+                FrameDev g = f;
+                g.Nb = 0;
+                if ((e = launch_plain_build_r(g, f.R, f.r_layout == COS_CAPON_R_REFERENCE ? 1 : 0, s))) return e;
+            }
+            ++i;
+        } else {
+            int e = run_plain(c, f, s);
+            if (e) return e;
+            ++i;
+        }
+    }
+    return 0;
+}
+
+static int read_status(cos_capon_ctx *c, cudaStream_t s, bool sync)
+{
+    if (sync) {
+        cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return e;
+    }
+    unsigned st = 0;
+    cudaError_t e = cudaMemcpy(&st, c->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return e;
+    if (st & ERR_TIMEOUT) {
+        cudaMemset(c->d_status, 0, sizeof(unsigned));
+        return COS_CAPON_ERR_TIMEOUT;
+    }
+    return 0;
+}
+
+extern "C" {
+
+int cos_capon_create(cos_capon_ctx **ctx)
+{
+    if (!ctx) return COS_CAPON_ERR_INVALID_VALUE;
+    *ctx = nullptr;
+    cos_capon_ctx *c = new (std::nothrow) cos_capon_ctx();
+    if (!c) return COS_CAPON_ERR_OUT_OF_MEMORY;
+    cudaError_t e = cudaGetDevice(&c->device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_status, sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMemset(c->d_status, 0, sizeof(unsigned));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        if (c->stream) cudaStreamDestroy(c->stream);
+        if (c->d_status) cudaFree(c->d_status);
+        delete c;
+        return e;
+    }
+    *ctx = c;
+    return 0;
+}
+
+int cos_capon_destroy(cos_capon_ctx *c)
+{
+    if (!c) return COS_CAPON_ERR_INVALID_VALUE;
+    cudaStreamSynchronize(c->stream);
+    for (DevBuf *b : {&c->x, &c->z, &c->P, &c->w, &c->R, &c->Rwork, &c->Ria, &c->A, &c->b, &c->sol}) b->release();
+    if (c->d_status) cudaFree(c->d_status);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return 0;
+}
+
+int cos_capon_run(cos_capon_ctx *c, const cos_capon_frame *frames, int nframes, const cos_capon_opts *opts,
+                  void *stream)
+{
+    if (!c || !frames || nframes < 1) return COS_CAPON_ERR_INVALID_VALUE;
+    const cos_capon_opts o = opts ? *opts : kDefaultOpts;
+    if (o.refine) return COS_CAPON_ERR_NOT_SUPPORTED;
+    std::vector<FrameDev> fs;
+    fs.reserve(nframes);
+    for (int i = 0; i < nframes; ++i) {
+        const cos_capon_frame &fr = frames[i];
+        int e = check_sizes(fr.L, fr.K, fr.M, fr.Nx, fr.Ny, fr.Nb);
+        if (e) return e;
+        if (!fr.x || !fr.z) return COS_CAPON_ERR_INVALID_VALUE;
+        fs.push_back(make_frame(fr, o));
+    }
+    cudaStream_t s = stream ? (cudaStream_t)stream : c->stream;
+    return run_frames(c, fs.data(), nframes, o, s);
+}
+
+int cos_capon_get_capon_ex(cos_capon_ctx *c, void *z, float *P, void *w, void *R, const void *x, float d, int L,
+                           int Yavg, int M, int Nx, int Nz, int Nb, const cos_capon_opts *opts)
+{
+    if (!c) return COS_CAPON_ERR_INVALID_VALUE;
+    int e = check_sizes(L, Yavg, M, Nx, Nz, Nb);
+    if (e) return e;
+    if (!x || !z) return COS_CAPON_ERR_INVALID_VALUE;
+    const cos_capon_opts o = opts ? *opts : kDefaultOpts;
+    if (o.refine) return COS_CAPON_ERR_NOT_SUPPORTED;
+    const size_t N = (size_t)Nx * Nz, npix = (size_t)Nx * (Nz - 2 * Yavg);
+    const size_t bx = N * M * sizeof(float2), bz = npix * sizeof(float2), bp = npix * sizeof(float),
+                 bw = npix * L * sizeof(float2), bR = npix * L * L * sizeof(float2);
+    const bool plain = !(o.form == COS_CAPON_FORM_FUSED && Nb == 0 && fused_supported(L));
+    size_t need = 0;
+    need += bx > c->x.cap ? bx : 0;
+    need += bz > c->z.cap ? bz : 0;
+    need += (P && bp > c->P.cap) ? bp : 0;
+    need += (w && bw > c->w.cap) ? bw : 0;
+    need += (R && bR > c->R.cap) ? bR : 0;
+    if (plain && Nb == 0) need += (bR > c->Rwork.cap ? bR : 0) + (bw > c->Ria.cap ? bw : 0);
+    if ((e = check_free(need))) return e;
+    if ((e = c->x.ensure(bx)) || (e = c->z.ensure(bz))) return e;
+    if (P && (e = c->P.ensure(bp))) return e;
+    if (w && (e = c->w.ensure(bw))) return e;
+    if (R && (e = c->R.ensure(bR))) return e;
+
+    cudaStream_t s = c->stream;
+    cudaError_t ce = cudaMemcpyAsync(c->x.p, x, bx, cudaMemcpyHostToDevice, s);
+    if (ce != cudaSuccess) return ce;
+    cos_capon_frame fr;
+    fr.x = c->x.p;
+    fr.z = c->z.p;
+    fr.P = P ? (float *)c->P.p : nullptr;
+    fr.w = w ? c->w.p : nullptr;
+    fr.R = R ? c->R.p : nullptr;
+    fr.d = d;
+    fr.L = L;
+    fr.K = Yavg;
+    fr.M = M;
+    fr.Nx = Nx;
+    fr.Ny = Nz;
+    fr.Nb = Nb;
+    if ((e = cos_capon_run(c, &fr, 1, &o, s))) return e;
+    if ((ce = cudaMemcpyAsync(z, c->z.p, bz, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return ce;
+    if (P && (ce = cudaMemcpyAsync(P, c->P.p, bp, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return ce;
+    if (w && (ce = cudaMemcpyAsync(w, c->w.p, bw, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return ce;
+    if (R && (ce = cudaMemcpyAsync(R, c->R.p, bR, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return ce;
+    return read_status(c, s, true);
+}
+
+int cos_capon_get_capon(cos_capon_ctx *c, void *z, void *w, void *R, const void *x, float d, int L, int Yavg, int M,
+                        int Nx, int Nz, int Nb)
+{
+    if (!w) return COS_CAPON_ERR_INVALID_VALUE;
+    return cos_capon_get_capon_ex(c, z, nullptr, w, R, x, d, L, Yavg, M, Nx, Nz, Nb, nullptr);
+}
+
+int cos_capon_build_r(cos_capon_ctx *c, void *R, const void *x, float d, int L, int Yavg, int M, int Nx, int Nz,
+                      int Nb, int R_on_gpu, int x_on_gpu)
+{
+    if (!c || !R || !x) return COS_CAPON_ERR_INVALID_VALUE;
+    int e = check_sizes(L, Yavg, M, Nx, Nz, Nb);
+    if (e) return e;
+    const int n = Nb > 0 ? Nb : L;
+    const size_t npix = (size_t)Nx * (Nz - 2 * Yavg);
+    const size_t bx = (size_t)Nx * Nz * M * sizeof(float2), bR = npix * n * n * sizeof(float2);
+    cudaStream_t s = c->stream;
+    const void *xd = x;
+    void *Rd = R;
+    cudaError_t ce;
+    if (!x_on_gpu) {
+        if ((e = c->x.ensure(bx))) return e;
+        if ((ce = cudaMemcpyAsync(c->x.p, x, bx, cudaMemcpyHostToDevice, s)) != cudaSuccess) return ce;
+        xd = c->x.p;
+    }
+    if (!R_on_gpu) {
+        if ((e = c->R.ensure(bR))) return e;
+        Rd = c->R.p;
+    }
+    cos_capon_frame fr;
+    memset(&fr, 0, sizeof(fr));
+    fr.x = xd;
+    fr.d = d;
+    fr.L = L;
+    fr.K = Yavg;
+    fr.M = M;
+    fr.Nx = Nx;
+    fr.Ny = Nz;
+    fr.Nb = Nb;
+    cos_capon_opts o = kDefaultOpts;
+    FrameDev f = make_frame(fr, o);
+    if (Nb > 0) {
+        // the reference's beamspace BuildR loads with tr(R_bs)/Nb (BuildR.cpp:82-86)
+        f.loading = COS_CAPON_LOAD_BEAMSPACE;
+        if ((e = launch_beamspace(f, (float2 *)Rd, s))) return e;
+    } else {
+        if ((e = launch_plain_build_r(f, (float2 *)Rd, 1, s))) return e;
+    }
+    if (!R_on_gpu && (ce = cudaMemcpyAsync(R, Rd, bR, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return ce;
+    return read_status(c, s, true);
+}
+
+int cos_capon_solve(cos_capon_ctx *c, void *x, const void *A, const void *b, int N, int batch, int x_on_gpu,
+                    int A_on_gpu, int b_on_gpu)
+{
+    if (!c || !x || !A || !b) return COS_CAPON_ERR_INVALID_VALUE;
+    // Solver.cpp:34-42
+    if (N < 1 || N > 72 || batch < 1) return COS_CAPON_ERR_LAUNCH;
+    const size_t bA = (size_t)N * N * batch * sizeof(float2), bv = (size_t)N * batch * sizeof(float2);
+    cudaStream_t s = c->stream;
+    cudaError_t ce;
+    int e;
+    const void *Ad = A, *bd = b;
+    void *xd = x;
+    if (!A_on_gpu) {
+        if ((e = c->A.ensure(bA))) return e;
+        if ((ce = cudaMemcpyAsync(c->A.p, A, bA, cudaMemcpyHostToDevice, s)) != cudaSuccess) return ce;
+        Ad = c->A.p;
+    }
+    if (!b_on_gpu) {
+        if ((e = c->b.ensure(bv))) return e;
+        if ((ce = cudaMemcpyAsync(c->b.p, b, bv, cudaMemcpyHostToDevice, s)) != cudaSuccess) return ce;
+        bd = c->b.p;
+    }
+    if (!x_on_gpu) {
+        if ((e = c->sol.ensure(bv))) return e;
+        xd = c->sol.p;
+    }
+    if ((e = launch_lu_solve((float2 *)xd, (const float2 *)Ad, (const float2 *)bd, N, batch, s))) return e;
+    if (!x_on_gpu && (ce = cudaMemcpyAsync(x, xd, bv, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return ce;
+    return read_status(c, s, true);
+}
+
+int cos_capon_butler(cos_capon_ctx *c, void *B, int Nb, int L, int B_on_gpu)
+{
+    if (!c || !B) return COS_CAPON_ERR_INVALID_VALUE;
+    if (Nb < 1 || L < 1 || Nb > L) return COS_CAPON_ERR_LAUNCH;
+    const size_t bytes = (size_t)Nb * L * sizeof(float2);
+    cudaStream_t s = c->stream;
+    void *Bd = B;
+    int e;
+    if (!B_on_gpu) {
+        if ((e = c->sol.ensure(bytes))) return e;
+        Bd = c->sol.p;
+    }
+    if ((e = launch_butler((float2 *)Bd, Nb, L, s))) return e;
+    cudaError_t ce;
+    if (!B_on_gpu && (ce = cudaMemcpyAsync(B, Bd, bytes, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return ce;
+    return read_status(c, s, true);
+}
+
+int cos_capon_device_status(cos_capon_ctx *c)
+{
+    if (!c) return COS_CAPON_ERR_INVALID_VALUE;
+    return read_status(c, c->stream, true);
+}
+
+const char *cos_capon_status_string(int st)
+{
+    switch (st) {
+    case COS_CAPON_SUCCESS: return "success";
+    case COS_CAPON_ERR_INVALID_VALUE: return "invalid value (NULL context or buffer)";
+    case COS_CAPON_ERR_OUT_OF_MEMORY: return "not enough device memory for the requested sizes";
+    case COS_CAPON_ERR_LAUNCH: return "invalid sizes (Nx, Nz, L, M < 1; Yavg, Nb < 0; Nb > L; L > M; 2*Yavg >= Nz; N outside [1, 72])";
+    case COS_CAPON_ERR_NOT_SUPPORTED: return "option or size outside what this build implements";
+    case COS_CAPON_ERR_TIMEOUT: return "a bounded device-side wait expired";
+    default: return cudaGetErrorString((cudaError_t)st);
+    }
+}
+
+}  // extern "C"

@@ -1,0 +1,238 @@
+// Beamspace Capon (Nb > 0) for sm_103a.
+//
+// Replaces the reference GPU beamspace routes (RealTimeCapon/Capon.cpp:285-417):
+// instead of building the L x L element-space R and transforming it with three
+// batched GEMMs (cublasCgemmBatched, Capon.cpp:599-650), every subarray
+// snapshot is reduced to Nb Butler beams by a sliding DFT
+// (sliding_beamspace_kernel.cu:26-82 recurrence)
+//     Y_{s+1}[b] = e^{+j 2 pi bin_b / L} * (Y_s[b] + (x[s+L] - x[s]) / sqrt(L)),
+// so that R_bs = B R B^H is formed directly as an Nb x Nb rank-(Ns*T) sum.
+// With element-space loading the loaded matrix is
+//     B (R + d tr(R)/L I) B^H = B R B^H + d tr(R)/L I      (B B^H = I),
+// and tr(R) comes from the snapshot energies; the beamspace-trace convention
+// loads with tr(R_bs)/Nb instead (getCaponAllC.pyx:376-385).  Then
+//     a_bs = B 1,  x_bs = R_bs^-1 a_bs,  Ria = B^H x_bs,
+//     w = Ria / sum(Ria),  z = sum conj(w) g  (capon_kernel.cu:338-427),
+//     P = 1 / Re(a_bs^H R_bs,normalised^-1 a_bs).
+// One warp per pixel.
+#include "capon_common.cuh"
+#include "capon_internal.h"
+#include "../../include/cos_capon.h"
+
+namespace cgb {
+
+static constexpr int kBsWarps = 4;
+
+struct BsSmem {
+    size_t per_warp, table, total;
+    int ld;  // Cm leading dimension
+    __host__ __device__ BsSmem(int M, int L, int K, int Nb)
+    {
+        const int T = 2 * K + 1, Ns = M - L + 1;
+        ld = Nb + 1;
+        per_warp = (size_t)T * M + (size_t)T * Ns * Nb + (size_t)Nb * ld + 2 * (size_t)Nb + 2;
+        table = (size_t)Nb * L + 2 * (size_t)Nb;
+        total = (table + kBsWarps * per_warp) * sizeof(float2);
+    }
+};
+
+__global__ void __launch_bounds__(32 * kBsWarps)
+beamspace_kernel(FrameDev f, float2 *__restrict__ Rbs)
+{
+    extern __shared__ float2 sm[];
+    const int M = f.M, L = f.L, K = f.K, T = 2 * K + 1, Ns = M - L + 1, Nb = f.Nb;
+    const BsSmem S(M, L, K, Nb);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float2 *Bt = sm;                        // Nb x L Butler matrix
+    float2 *rot = Bt + (size_t)Nb * L;      // Nb sliding factors
+    float2 *ab = rot + Nb;                  // a_bs = B 1
+    float2 *ws = sm + S.table + (size_t)warp * S.per_warp;
+    float2 *xs = ws;                              // T x M
+    float2 *Y = xs + (size_t)T * M;               // T x Ns x Nb
+    float2 *Cm = Y + (size_t)T * Ns * Nb;         // Nb x ld
+    float2 *xb = Cm + (size_t)Nb * S.ld;          // Nb
+    const float isl = 1.0f / sqrtf((float)L);
+
+    for (int i = threadIdx.x; i < Nb * L; i += blockDim.x) {
+        const int bb = i / L, l = i % L;
+        const int bin = butler_bin(bb, Nb, L);
+        float sn, cs;
+        sincospif(2.0f * (float)((bin * l) % L) / (float)L, &sn, &cs);
+        Bt[i] = make_float2(cs * isl, -sn * isl);
+    }
+    for (int bb = threadIdx.x; bb < Nb; bb += blockDim.x) {
+        float sn, cs;
+        sincospif(2.0f * (float)butler_bin(bb, Nb, L) / (float)L, &sn, &cs);
+        rot[bb] = make_float2(cs, sn);
+    }
+    __syncthreads();
+    for (int bb = warp; bb < Nb; bb += kBsWarps) {
+        float2 acc = make_float2(0.f, 0.f);
+        for (int l = lane; l < L; l += 32) acc = cadd(acc, Bt[bb * L + l]);
+        for (int o = 16; o; o >>= 1) acc = cadd(acc, shfl2_xor(acc, o, 32));
+        if (lane == 0) ab[bb] = acc;
+    }
+    __syncthreads();
+
+    const long long npix = (long long)f.Nx * f.Npy;
+    const long long pix = (long long)blockIdx.x * kBsWarps + warp;
+    if (pix >= npix) return;
+    const int bx = (int)(pix / f.Npy), p = (int)(pix % f.Npy);
+    const float2 *xg = f.x + ((size_t)bx * f.Ny + p) * M;
+    for (int i = lane; i < T * M; i += 32) xs[i] = xg[i];
+    __syncwarp();
+
+    // sliding DFT over a contiguous chunk of subarrays per lane
+    const int chunk = (Ns + 31) / 32;
+    const int s0 = lane * chunk, s1 = min(Ns, s0 + chunk);
+    float energy = 0.f;  // sum over the lane's subarrays of |x_t[s:s+L]|^2
+    for (int t = 0; t < T && s0 < s1; ++t) {
+        const float2 *xt = xs + t * M;
+        float e = 0.f;
+        for (int l = 0; l < L; ++l) e += cabs2(xt[s0 + l]);
+        energy += e;
+        for (int s = s0 + 1; s < s1; ++s) {
+            e += cabs2(xt[s - 1 + L]) - cabs2(xt[s - 1]);
+            energy += e;
+        }
+        for (int bb = 0; bb < Nb; ++bb) {
+            float2 acc = make_float2(0.f, 0.f);
+            for (int l = 0; l < L; ++l) acc = cadd(acc, cmul(Bt[bb * L + l], xt[s0 + l]));
+            Y[((size_t)t * Ns + s0) * Nb + bb] = acc;
+            const float2 rb = rot[bb];
+            for (int s = s0 + 1; s < s1; ++s) {
+                acc = cmul(rb, cadd(acc, cscale(csub(xt[s - 1 + L], xt[s - 1]), isl)));
+                Y[((size_t)t * Ns + s) * Nb + bb] = acc;
+            }
+        }
+    }
+    for (int o = 16; o; o >>= 1) energy += __shfl_xor_sync(0xffffffffu, energy, o);
+    __syncwarp();
+
+    // Nb x Nb covariance, upper triangle by lanes, mirrored
+    const int ne = Nb * (Nb + 1) / 2;
+    for (int e = lane; e < ne; e += 32) {
+        int bb = 0, rem = e;
+        while (rem >= Nb - bb) { rem -= Nb - bb; ++bb; }
+        const int cc = bb + rem;
+        float2 acc = make_float2(0.f, 0.f);
+        for (int q = 0; q < T * Ns; ++q) acc = cadd(acc, cmulc(Y[(size_t)q * Nb + bb], Y[(size_t)q * Nb + cc]));
+        Cm[bb * S.ld + cc] = acc;
+        Cm[cc * S.ld + bb] = cconj(acc);
+    }
+    __syncwarp();
+    if (lane == 0) {
+        float dl;
+        if (f.loading == COS_CAPON_LOAD_BEAMSPACE) {
+            float tb = 0.f;
+            for (int i = 0; i < Nb; ++i) tb += Cm[i * S.ld + i].x;
+            dl = f.d * tb / (float)Nb;
+        } else {
+            dl = f.d * energy / (float)L;
+        }
+        for (int i = 0; i < Nb; ++i) Cm[i * S.ld + i] = make_float2(Cm[i * S.ld + i].x + dl, 0.f);
+    }
+    __syncwarp();
+    if (Rbs) {  // loaded, unnormalised, column-major (as the reference BuildR writes R)
+        float2 *Rp = Rbs + (size_t)pix * Nb * Nb;
+        for (int i = lane; i < Nb * Nb; i += 32) Rp[i] = Cm[(i % Nb) * S.ld + i / Nb];
+    }
+    __syncwarp();
+    // Cholesky (upper, row-major in Cm) and the two triangular solves for a_bs
+    if (lane == 0) {
+        for (int i = 0; i < Nb; ++i) {
+            float dv = Cm[i * S.ld + i].x;
+            for (int k = 0; k < i; ++k) dv -= cabs2(Cm[k * S.ld + i]);
+            const float u = sqrtf(dv), iu = 1.0f / u;
+            Cm[i * S.ld + i] = make_float2(u, 0.f);
+            for (int j = i + 1; j < Nb; ++j) {
+                float2 v = Cm[i * S.ld + j];
+                for (int k = 0; k < i; ++k) v = csub(v, cconjmul(Cm[k * S.ld + i], Cm[k * S.ld + j]));
+                Cm[i * S.ld + j] = cscale(v, iu);
+            }
+        }
+        for (int i = 0; i < Nb; ++i) {
+            float2 v = ab[i];
+            for (int k = 0; k < i; ++k) v = csub(v, cconjmul(Cm[k * S.ld + i], xb[k]));
+            xb[i] = cscale(v, 1.0f / Cm[i * S.ld + i].x);
+        }
+        for (int i = Nb - 1; i >= 0; --i) {
+            float2 v = xb[i];
+            for (int k = i + 1; k < Nb; ++k) v = csub(v, cmul(Cm[i * S.ld + k], xb[k]));
+            xb[i] = cscale(v, 1.0f / Cm[i * S.ld + i].x);
+        }
+    }
+    __syncwarp();
+    // Ria = B^H x_bs, w = Ria / sum(Ria), z = sum conj(w) g
+    float2 ria[2], sum = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        const int l = lane + 32 * q;
+        ria[q] = make_float2(0.f, 0.f);
+        if (l < L) {
+            for (int bb = 0; bb < Nb; ++bb) ria[q] = cadd(ria[q], cconjmul(Bt[bb * L + l], xb[bb]));
+            sum = cadd(sum, ria[q]);
+        }
+    }
+    for (int o = 16; o; o >>= 1) sum = cadd(sum, shfl2_xor(sum, o, 32));
+    const float den = cabs2(sum);
+    const float2 isum = make_float2(sum.x / den, -sum.y / den);
+    const float2 *xc = xs + (size_t)K * M;
+    const float invNs = 1.0f / (float)Ns;
+    float2 zacc = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        const int l = lane + 32 * q;
+        if (l < L) {
+            const float2 wl = cmul(ria[q], isum);
+            if (f.w) f.w[(size_t)pix * L + l] = wl;
+            float2 g = make_float2(0.f, 0.f);
+            for (int s = 0; s < Ns; ++s) g = cadd(g, xc[s + l]);
+            zacc = cadd(zacc, cconjmul(wl, cscale(g, invNs)));
+        }
+    }
+    for (int o = 16; o; o >>= 1) zacc = cadd(zacc, shfl2_xor(zacc, o, 32));
+    if (lane == 0) {
+        if (f.z) f.z[pix] = zacc;
+        if (f.P) {
+            float2 aRa = make_float2(0.f, 0.f);
+            for (int bb = 0; bb < Nb; ++bb) aRa = cadd(aRa, cconjmul(ab[bb], xb[bb]));
+            f.P[pix] = 1.0f / ((float)Ns * (float)T * aRa.x);
+        }
+    }
+}
+
+int launch_beamspace(const FrameDev &f, float2 *R_out, cudaStream_t s)
+{
+    if (f.L > 64) return cudaErrorNotSupported;
+    const BsSmem S(f.M, f.L, f.K, f.Nb);
+    if (S.total > 227 * 1024) return cudaErrorNotSupported;
+    cudaError_t e = cudaFuncSetAttribute(beamspace_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)S.total);
+    if (e != cudaSuccess) return e;
+    const long long npix = (long long)f.Nx * f.Npy;
+    const long long blocks = (npix + kBsWarps - 1) / kBsWarps;
+    beamspace_kernel<<<(unsigned)blocks, 32 * kBsWarps, S.total, s>>>(f, R_out);
+    return cudaGetLastError();
+}
+
+__global__ void butler_kernel(float2 *B, int Nb, int L)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= Nb * L) return;
+    const int bb = i / L, l = i % L;
+    const int bin = butler_bin(bb, Nb, L);
+    float sn, cs;
+    sincospif(2.0f * (float)((bin * l) % L) / (float)L, &sn, &cs);
+    const float isl = 1.0f / sqrtf((float)L);
+    B[i] = make_float2(cs * isl, -sn * isl);
+}
+
+int launch_butler(float2 *B, int Nb, int L, cudaStream_t s)
+{
+    const int n = Nb * L;
+    butler_kernel<<<(n + 127) / 128, 128, 0, s>>>(B, Nb, L);
+    return cudaGetLastError();
+}
+
+}  // namespace cgb

@@ -1,0 +1,60 @@
+// Internal interfaces between the host API (capon_api.cu) and the kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace cgb {
+
+// Device-side description of one frame.  Pixel p of beam bx sits at range
+// row p + K; its snapshots are rows p .. p+2K.
+struct FrameDev {
+    const float2 *x;   // [Nx][Ny][M]
+    float2 *z;         // [Nx][Npy]
+    float *P;          // [Nx][Npy] or null
+    float2 *w;         // [Nx][Npy][L] or null
+    float2 *R;         // [Nx][Npy][L][L] or null
+    float d;
+    int L, K, M, Nx, Ny, Nb;
+    int Npy;           // Ny - 2K pixels per beam
+    int loading;       // COS_CAPON_LOAD_*
+    int r_layout;      // COS_CAPON_R_*
+    int refine;
+    int tile;          // pixels per range tile (kernel-specific)
+    int tiles_per_beam;
+    long long tile_begin;  // first global tile index of this frame
+};
+
+// Frame descriptors passed by value as a kernel parameter (graph-capturable).
+static constexpr int kMaxFrames = 8;
+struct FramesParam {
+    FrameDev f[kMaxFrames];
+    int n;
+};
+
+// Error bits written to the device status word.
+enum : unsigned { ERR_TIMEOUT = 1u, ERR_NOT_PD = 2u };
+
+// Bounded wait on a shared-memory mbarrier phase; returns false after
+// `limit` polls (the caller records ERR_TIMEOUT and leaves).
+static constexpr uint32_t kWaitLimit = 1u << 22;
+
+// ---- launchers (return cudaError_t as int) ----------------------------------
+// plain three-stage element-space pipeline; R_work must hold Nx*Npy*L*L complex
+int launch_plain_build_r(const FrameDev &f, float2 *R_out, int r_ref_layout, cudaStream_t s);
+int launch_plain_solve_hpd(const FrameDev &f, const float2 *R, float2 *Ria, unsigned *status,
+                           cudaStream_t s);
+int launch_plain_output(const FrameDev &f, const float2 *Ria, cudaStream_t s);
+// general batched LU solve, column-major A
+int launch_lu_solve(float2 *x, const float2 *A, const float2 *b, int N, int batch, cudaStream_t s);
+// fused element-space path; returns cudaErrorNotSupported when L has no instantiation.
+// fp.f[i].tile_begin / tiles_per_beam must use fused_tile(L)-sized tiles; all
+// frames of one launch share L, K and M.
+bool fused_supported(int L);
+int fused_tile(int L);
+int fused_tmax(int L);  // largest 2K+1 the instantiation holds
+int launch_fused_frames(const FramesParam &fp, unsigned *status, int num_sms, cudaStream_t s);
+// beamspace path (Nb > 0)
+int launch_beamspace(const FrameDev &f, float2 *R_out, cudaStream_t s);
+int launch_butler(float2 *B, int Nb, int L, cudaStream_t s);
+
+}  // namespace cgb

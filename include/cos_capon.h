@@ -1,0 +1,136 @@
+/*
+ * cos_capon.h -- C ABI of the GB300-native Capon/MVDR per-pixel path.
+ *
+ * Plain pointers and sizes only.  Complex samples are interleaved float pairs
+ * {re, im} (the reference's Complex<float>, framework/lib/Complex.h:12-166).
+ * Every function returns an int status: 0 on success, otherwise one of the
+ * COS_CAPON_* codes below, whose values are the CUDA runtime error numbers the
+ * reference returns in the same situations.
+ *
+ * Array conventions (reference getCaponC.pyx:74-83, Capon.cpp:93-94):
+ *   x  input cube      complex64 [Nx][Nz][M]        (beam, range, channel)
+ *   z  amplitude       complex64 [Nx][Nz-2*Yavg]
+ *   P  power           float32   [Nx][Nz-2*Yavg]   (1 / Re(a^H R_d^-1 a), R_d normalised)
+ *   w  weights         complex64 [Nx][Nz-2*Yavg][L]
+ *   R  covariance      complex64 [Nx][Nz-2*Yavg][L][L]
+ * Range rows 0..Yavg-1 and Nz-Yavg..Nz-1 produce no pixel.
+ */
+#ifndef COS_CAPON_H
+#define COS_CAPON_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define COS_CAPON_SUCCESS           0    /* cudaSuccess                                           */
+#define COS_CAPON_ERR_INVALID_VALUE 1    /* cudaErrorInvalidValue: NULL context or buffer         */
+#define COS_CAPON_ERR_OUT_OF_MEMORY 32   /* cudaErrorMemoryValueTooLarge (Capon.cpp:116-133)       */
+#define COS_CAPON_ERR_LAUNCH        719  /* cudaErrorLaunchFailure: invalid sizes (Capon.cpp:98-107,
+                                            BuildR.cpp:37-48, Solver.cpp:34-42)                    */
+#define COS_CAPON_ERR_NOT_SUPPORTED 801  /* cudaErrorNotSupported: option outside what is built     */
+#define COS_CAPON_ERR_TIMEOUT       909  /* cudaErrorTimeout: a bounded device-side wait expired   */
+
+/* ---- options ------------------------------------------------------------ */
+#define COS_CAPON_FORM_FUSED   0  /* one fused persistent kernel per launch (default)             */
+#define COS_CAPON_FORM_PLAIN   1  /* plain FP32 three-stage pipeline: build R -> solve -> output   */
+
+#define COS_CAPON_LOAD_ELEMENT   0  /* R_d = R + d*tr(R)/L*I before any beamspace transform
+                                       (reference GPU default, buildR_kernel.cu:153-154)          */
+#define COS_CAPON_LOAD_BEAMSPACE 1  /* load after the transform with tr(R_bs)/Nb
+                                       (getCaponAllC.pyx:376-385; sliding route BuildR.cpp:82-86) */
+
+#define COS_CAPON_R_REFERENCE  0  /* R as the reference GPU writes it: per pixel column-major,
+                                     loaded, not normalised (buildR_kernel.cu:84-86,153-157)       */
+#define COS_CAPON_R_NORMALISED 1  /* R row-major, loaded, normalised by 1/((M-L+1)(2Yavg+1))
+                                     (getCaponC.pyx:240-242)                                     */
+
+typedef struct cos_capon_opts {
+    int form;       /* COS_CAPON_FORM_*                                       */
+    int loading;    /* COS_CAPON_LOAD_*                                       */
+    int r_layout;   /* COS_CAPON_R_*                                          */
+    int refine;     /* 1: one step of iterative refinement of R^-1 a with an
+                       FP64 residual; 0: plain FP32 Cholesky                  */
+} cos_capon_opts;
+
+/* One frame (data cube + parameters) of a device-pointer call. */
+typedef struct cos_capon_frame {
+    const void *x;  /* device, complex64 [Nx][Ny][M]                          */
+    void *z;        /* device, complex64 [Nx][Ny-2K]           (required)     */
+    float *P;       /* device, float32   [Nx][Ny-2K]           or NULL        */
+    void *w;        /* device, complex64 [Nx][Ny-2K][L]        or NULL        */
+    void *R;        /* device, complex64 [Nx][Ny-2K][L][L]     or NULL        */
+    float d;        /* diagonal loading coefficient (relative to trace)       */
+    int L;          /* subarray length                                        */
+    int K;          /* temporal half window: 2K+1 range samples               */
+    int M;          /* channels                                               */
+    int Nx;         /* beams                                                  */
+    int Ny;         /* range samples                                          */
+    int Nb;         /* beamspace dimension, 0 = element space                 */
+} cos_capon_frame;
+
+typedef struct cos_capon_ctx cos_capon_ctx;
+
+/* Create / destroy a context.  The context owns the device buffers of the
+ * host-pointer calls (grown on demand, freed by destroy), its stream and its
+ * device status word -- the role of the reference's Capon object
+ * (Capon.h:13-125, Capon.cpp:50-71).  Uses the calling thread's current device. */
+int cos_capon_create(cos_capon_ctx **ctx);
+int cos_capon_destroy(cos_capon_ctx *ctx);
+
+/* Drop-in for ICapon<Complex<float>,float>::getCapon (ICapon.h:20-33) and its
+ * implementation Capon::getCapon (Capon.cpp:73-152): host pointers, synchronous.
+ * z and w are required; R may be NULL (the reference copies it back only under
+ * COPY_R_DEVICE_HOST, Capon.cpp:9,253-259) and is written in the reference GPU
+ * convention (COS_CAPON_R_REFERENCE).  d, L, Yavg, M, Nx, Nz, Nb mean what they
+ * mean there; Nb > 0 selects beamspace with element-space loading. */
+int cos_capon_get_capon(cos_capon_ctx *ctx, void *z, void *w, void *R, const void *x,
+                        float d, int L, int Yavg, int M, int Nx, int Nz, int Nb);
+
+/* Same call with the output power P (float32, may be NULL), optional w / R and
+ * explicit options (NULL = defaults).  Host pointers, synchronous.  This is the
+ * call behind the Python getCaponCUDAPy / getCaponCPy mirrors. */
+int cos_capon_get_capon_ex(cos_capon_ctx *ctx, void *z, float *P, void *w, void *R,
+                           const void *x, float d, int L, int Yavg, int M, int Nx, int Nz,
+                           int Nb, const cos_capon_opts *opts);
+
+/* Device-pointer call: every pixel of `nframes` frames (each with its own M, L,
+ * K, Nb) in one launch on `stream` (a cudaStream_t, NULL = the context's
+ * stream).  Asynchronous; no host synchronisation and no allocation once the
+ * context has served a call of the same or larger shape, so it can be captured
+ * into a CUDA graph after one warm-up call. */
+int cos_capon_run(cos_capon_ctx *ctx, const cos_capon_frame *frames, int nframes,
+                  const cos_capon_opts *opts, void *stream);
+
+/* Drop-in for IBuildR::getR (IBuildR.h:85-98) / BuildR::getR (BuildR.cpp:21-106):
+ * covariance with spatial smoothing, temporal averaging and diagonal loading,
+ * written per pixel column-major and not normalised, as the reference does.
+ * With Nb > 0, R is Nb x Nb in the Butler beamspace (element-space loading).
+ * R_on_gpu / x_on_gpu: nonzero when that pointer is device memory. */
+int cos_capon_build_r(cos_capon_ctx *ctx, void *R, const void *x, float d, int L, int Yavg,
+                      int M, int Nx, int Nz, int Nb, int R_on_gpu, int x_on_gpu);
+
+/* Drop-in for ISolver::solve (ISolver.h:119-128) / Solver::solve (Solver.cpp:23-116):
+ * `batch` dense N x N complex systems A x = b, A column-major per system (the
+ * layout the reference's BuildR produces and its solver reads), 1 <= N <= 72,
+ * solved by LU with partial pivoting, so A need not be Hermitian. */
+int cos_capon_solve(cos_capon_ctx *ctx, void *x, const void *A, const void *b, int N, int batch,
+                    int x_on_gpu, int A_on_gpu, int b_on_gpu);
+
+/* Butler (normalised DFT) beamspace matrix, Nb x L, row-major, host or device
+ * pointer (B_on_gpu): B[b,l] = exp(-j*2*pi*bin(b)*l/L)/sqrt(L) with the beam
+ * layout of capon_kernel.cu:47-77 (butler_matrix). */
+int cos_capon_butler(cos_capon_ctx *ctx, void *B, int Nb, int L, int B_on_gpu);
+
+/* Status word of the last launch on this context (0, or COS_CAPON_ERR_TIMEOUT
+ * when a bounded device-side wait gave up).  Synchronises the context stream. */
+int cos_capon_device_status(cos_capon_ctx *ctx);
+
+/* Human-readable text for a status code. */
+const char *cos_capon_status_string(int status);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* COS_CAPON_H */

@@ -1,0 +1,347 @@
+/*
+ * FP64 CPU restatement of the reference's Capon/MVDR per-pixel path.
+ *
+ * TEST INFRASTRUCTURE ONLY: this is the oracle the CUDA path is checked
+ * against (tests, smoke check) and the "port" CPU baseline of the benchmark.
+ * The product never links or calls it.
+ *
+ * Element space follows framework/beamformer/capon/getCaponC.pyx:
+ *   snapshot gather            :203-205
+ *   band covariance R_full     :207-223
+ *   spatial smoothing + conj   :226-242   (R[j,k] = sum_s R_full[s+j,s+k], k>=j)
+ *   subarray sums g            :246-255
+ *   diagonal loading           :257-262   (R += regCoef*trace(R)/L * I)
+ *   solve (Cholesky)           :274       -> framework/linalg/linearSolvec.pyx:259-282
+ *   weights / amplitude        :276-283
+ *   power (upper-triangle sum) :285-289   (the reference's "zPow", see below)
+ * Cholesky / triangular solves follow framework/linalg/matrixDecompc.pyx:19-50
+ * and framework/linalg/linearSolvec.pyx:312-346.
+ *
+ * The reference declares regCoef, K_inv and norm_inv as C float
+ * (getCaponC.pyx:79,129-132).  `fp32_scalars=1` reproduces that rounding,
+ * `fp32_scalars=0` gives the pure-FP64 definition.
+ *
+ * Output power.  The reference's zPow sums only the upper triangle of the
+ * loaded covariance, because its R has an empty lower triangle
+ * (getCaponC.pyx:180, 231-242, 285-289).  Both are returned:
+ *   zpow_ref = sum_{i} sum_{j>=i} conj(w_j) R[i,j] w_i        (complex)
+ *   P        = w^H R w = 1 / Re(a^H R^-1 a)                    (real, true MVDR power)
+ *
+ * Beamspace follows the reference GPU default route,
+ * framework/beamformer/capon/RealTimeCapon/Capon.cpp:285-410:
+ * Butler matrix B (Nb x L) per capon_kernel.cu:47-77 (beam b <= Nb/2 -> DFT bin b,
+ * otherwise bin b + L - 2*(Nb/2) - 1; B[b,l] = exp(-j 2 pi bin l / L)/sqrt(L)),
+ * element-space loading (buildR_kernel.cu:153-154), R_bs = B R_d B^H,
+ * a_bs = B 1, Ria = B^H R_bs^-1 a_bs, then the element-space output step
+ * (w = Ria / sum(Ria), z = sum conj(w) g; capon_kernel.cu:338-427).
+ * `bs_loading = 1` instead loads after the transform with trace(R_bs)/Nb, the
+ * convention of framework/beamformer/capon/getCaponAllC.pyx:376-385.
+ */
+#define _GNU_SOURCE
+#include <complex.h>
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+typedef double _Complex cplx;
+
+static const double kPi = 3.14159265358979323846;
+
+/* ---- small dense kernels (matrixDecompc.pyx / linearSolvec.pyx) ---------- */
+
+/* Upper Cholesky factor U (row-major n x n) with U^H U = A; reads A's upper
+ * triangle only.  matrixDecompc.pyx:19-50 (complex square root of the pivot). */
+void oracle_cholesky(const cplx *A, int n, cplx *U)
+{
+    memset(U, 0, sizeof(cplx) * (size_t)n * n);
+    for (int i = 0; i < n; ++i) {
+        cplx s = 0;
+        for (int k = 0; k < i; ++k) s += U[k * n + i] * conj(U[k * n + i]);
+        U[i * n + i] = csqrt(A[i * n + i] - s);
+        for (int j = i + 1; j < n; ++j) {
+            cplx t = 0;
+            for (int k = 0; k < i; ++k) t += conj(U[k * n + i]) * U[k * n + j];
+            U[i * n + j] = (A[i * n + j] - t) / U[i * n + i];
+        }
+    }
+}
+
+/* Lower-triangular solve A x = b (linearSolvec.pyx:312-327). */
+void oracle_forward_solve(const cplx *A, const cplx *b, int n, cplx *x)
+{
+    for (int i = 0; i < n; ++i) {
+        cplx v = b[i];
+        for (int k = 0; k < i; ++k) v -= A[i * n + k] * x[k];
+        x[i] = v / A[i * n + i];
+    }
+}
+
+/* Upper-triangular solve A x = b (linearSolvec.pyx:330-346). */
+void oracle_back_solve(const cplx *A, const cplx *b, int n, cplx *x)
+{
+    for (int i = n - 1; i >= 0; --i) {
+        cplx v = b[i];
+        for (int k = n - 1; k > i; --k) v -= A[i * n + k] * x[k];
+        x[i] = v / A[i * n + i];
+    }
+}
+
+/* solveCholesky: U = chol(A); y = (U^H)^-1 b; x = U^-1 y (linearSolvec.pyx:259-282).
+ * `work` holds 2*n*n + n elements. */
+void oracle_solve_cholesky(const cplx *A, const cplx *b, int n, cplx *x, cplx *work)
+{
+    cplx *U = work, *UT = work + (size_t)n * n, *y = work + 2 * (size_t)n * n;
+    oracle_cholesky(A, n, U);
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) UT[j * n + i] = conj(U[i * n + j]);
+    oracle_forward_solve(UT, b, n, y);
+    oracle_back_solve(U, y, n, x);
+}
+
+/* DFT bin of beam b (capon_kernel.cu:53-59; the even-Nb branch there is dead code). */
+static int butler_bin(int b, int Nb, int L)
+{
+    return (b > Nb / 2) ? b + (L - 2 * (Nb / 2) - 1) : b;
+}
+
+/* Butler matrix, row-major Nb x L.  symmetric=1: the GPU beam layout of
+ * capon_kernel.cu:47-77; symmetric=0: the first Nb DFT bins, as
+ * framework/linalg/beamspace.py:18-34 (butlerMatrix) lays them out. */
+void oracle_butler_layout(int Nb, int L, cplx *B, int symmetric)
+{
+    for (int b = 0; b < Nb; ++b) {
+        int bin = symmetric ? butler_bin(b, Nb, L) : b;
+        for (int l = 0; l < L; ++l)
+            B[b * L + l] = cexp(-I * 2.0 * kPi * (double)bin * (double)l / (double)L) / sqrt((double)L);
+    }
+}
+
+/* Butler matrix in the GPU beam layout (capon_kernel.cu:47-77). */
+void oracle_butler(int Nb, int L, cplx *B)
+{
+    for (int b = 0; b < Nb; ++b) {
+        int bin = butler_bin(b, Nb, L);
+        for (int l = 0; l < L; ++l)
+            B[b * L + l] = cexp(-I * 2.0 * kPi * (double)bin * (double)l / (double)L) / sqrt((double)L);
+    }
+}
+
+/* ---- the per-pixel path -------------------------------------------------- */
+
+typedef struct {
+    const float *Xd;   /* interleaved complex64 [Nx][Ny][M] */
+    int Nx, Ny, M, L, Navg, Nb, fp32_scalars, bs_loading;
+    double regCoef;
+    /* outputs (any may be NULL except z): [Nx][Ny-2Navg](...) */
+    cplx *z, *zpow, *w, *R;
+    double *P;
+    int x0, x1;        /* beam range for this worker */
+} job_t;
+
+static void pixel_run(const job_t *jb, int x, int y, cplx *scratch)
+{
+    const int M = jb->M, L = jb->L, Navg = jb->Navg, Ny = jb->Ny, Nb = jb->Nb;
+    const int T = 2 * Navg + 1, Ns = M - L + 1;
+    const int Npy = Ny - 2 * Navg;
+    const size_t pix = (size_t)x * Npy + (size_t)(y - Navg);
+
+    double regCoef = jb->regCoef, K_inv = 1.0 / Ns, norm_inv = 1.0 / ((double)Ns * T);
+    if (jb->fp32_scalars) {
+        regCoef = (float)regCoef;
+        K_inv = (float)(1.0f / (float)Ns);
+        norm_inv = (float)(1.0f / ((float)Ns * (float)T));
+    }
+
+    cplx *ar = scratch;                       /* T x M   */
+    cplx *Rf = ar + (size_t)T * M;            /* M x M   */
+    cplx *R = Rf + (size_t)M * M;             /* L x L   */
+    cplx *g = R + (size_t)L * L;              /* L       */
+    cplx *a = g + L;                          /* L       */
+    cplx *Ria = a + L;                        /* L       */
+    cplx *wk = Ria + L;                       /* 2 L L + L */
+    cplx *wv = wk + 2 * (size_t)L * L + L;    /* L       */
+
+    /* :203-205 snapshot gather */
+    for (int t = 0; t < T; ++t)
+        for (int m = 0; m < M; ++m) {
+            const float *p = jb->Xd + 2 * (((size_t)x * Ny + (y - Navg + t)) * M + m);
+            ar[t * M + m] = (double)p[0] + I * (double)p[1];
+        }
+    /* :207-223 band of R_full = ar^H ar, R_full[i, i+j] for 0 <= j < L */
+    for (int i = 0; i < M; ++i)
+        for (int j = 0; j < L && i + j < M; ++j) {
+            cplx s = 0;
+            for (int t = 0; t < T; ++t) s += conj(ar[t * M + i]) * ar[t * M + i + j];
+            Rf[i * M + i + j] = s;
+        }
+    /* :226-242 smoothing over subarrays (upper triangle), then conj / norm */
+    for (int j = 0; j < L; ++j)
+        for (int k = 0; k < L; ++k) R[j * L + k] = 0;
+    for (int s = 0; s < Ns; ++s)
+        for (int j = 0; j < L; ++j)
+            for (int k = j; k < L; ++k) R[j * L + k] += Rf[(s + j) * M + s + k];
+    for (int j = 0; j < L; ++j)
+        for (int k = j; k < L; ++k) R[j * L + k] = conj(R[j * L + k]) * norm_inv;
+
+    /* :246-255 subarray sums of the centre snapshot */
+    {
+        cplx s0 = 0;
+        const cplx *xc = ar + (size_t)Navg * M;
+        for (int i = 0; i < Ns; ++i) s0 += xc[i];
+        g[0] = s0;
+        for (int i = 1; i < L; ++i) g[i] = g[i - 1] - xc[i - 1] + xc[M - L + i];
+        for (int i = 0; i < L; ++i) g[i] *= K_inv;
+    }
+
+    /* full Hermitian R (lower from upper) for the solve and the outputs */
+    for (int j = 0; j < L; ++j)
+        for (int k = 0; k < j; ++k) R[j * L + k] = conj(R[k * L + j]);
+
+    cplx zz = 0, zp = 0;
+    double Pv;
+    if (Nb <= 0) {
+        /* :257-262 diagonal loading */
+        cplx tr = 0;
+        for (int i = 0; i < L; ++i) tr += R[i * L + i];
+        cplx dl = tr * regCoef / L;
+        for (int i = 0; i < L; ++i) R[i * L + i] += dl;
+        for (int i = 0; i < L; ++i) a[i] = 1.0;
+        /* :274 */
+        oracle_solve_cholesky(R, a, L, Ria, wk);
+        /* :276-283 */
+        cplx aRia = 0;
+        for (int i = 0; i < L; ++i) aRia += conj(a[i]) * Ria[i];
+        for (int i = 0; i < L; ++i) wv[i] = Ria[i] / aRia;
+        for (int i = 0; i < L; ++i) zz += conj(wv[i]) * g[i];
+        /* :285-289 upper-triangle quirk */
+        for (int i = 0; i < L; ++i) {
+            cplx idot = 0;
+            for (int j = i; j < L; ++j) idot += conj(wv[j]) * R[i * L + j];
+            zp += idot * wv[i];
+        }
+        Pv = 1.0 / creal(aRia);
+    } else {
+        /* beamspace: R_bs = B R_d B^H (Capon.cpp:311-319) */
+        cplx *B = wk;                                  /* Nb x L */
+        cplx *Rb = B + (size_t)Nb * L;                 /* Nb x Nb */
+        cplx *tmp = Rb + (size_t)Nb * Nb;              /* Nb x L */
+        cplx *ab = tmp + (size_t)Nb * L;               /* Nb */
+        cplx *xb = ab + Nb;                            /* Nb */
+        cplx *wb = xb + Nb;                            /* 2 Nb Nb + Nb */
+        oracle_butler(Nb, L, B);
+        if (!jb->bs_loading) {
+            cplx tr = 0;
+            for (int i = 0; i < L; ++i) tr += R[i * L + i];
+            cplx dl = tr * regCoef / L;
+            for (int i = 0; i < L; ++i) R[i * L + i] += dl;
+        }
+        for (int b = 0; b < Nb; ++b)
+            for (int l = 0; l < L; ++l) {
+                cplx s = 0;
+                for (int k = 0; k < L; ++k) s += B[b * L + k] * R[k * L + l];
+                tmp[b * L + l] = s;
+            }
+        for (int b = 0; b < Nb; ++b)
+            for (int c = 0; c < Nb; ++c) {
+                cplx s = 0;
+                for (int l = 0; l < L; ++l) s += tmp[b * L + l] * conj(B[c * L + l]);
+                Rb[b * Nb + c] = s;
+            }
+        if (jb->bs_loading) {   /* getCaponAllC.pyx:376-385 */
+            cplx tr = 0;
+            for (int i = 0; i < Nb; ++i) tr += Rb[i * Nb + i];
+            cplx dl = tr * regCoef / Nb;
+            for (int i = 0; i < Nb; ++i) Rb[i * Nb + i] += dl;
+        }
+        for (int b = 0; b < Nb; ++b) {               /* a_bs = B 1 (Capon.cpp:329-333) */
+            cplx s = 0;
+            for (int l = 0; l < L; ++l) s += B[b * L + l];
+            ab[b] = s;
+        }
+        oracle_solve_cholesky(Rb, ab, Nb, xb, wb);
+        for (int l = 0; l < L; ++l) {                 /* Ria = B^H Ria_bs (Capon.cpp:366-369) */
+            cplx s = 0;
+            for (int b = 0; b < Nb; ++b) s += conj(B[b * L + l]) * xb[b];
+            Ria[l] = s;
+        }
+        cplx sum = 0;                                 /* capon_kernel.cu:373-379 */
+        for (int l = 0; l < L; ++l) sum += Ria[l];
+        for (int l = 0; l < L; ++l) wv[l] = Ria[l] / sum;
+        for (int l = 0; l < L; ++l) zz += conj(wv[l]) * g[l];
+        cplx aRia = 0;
+        for (int b = 0; b < Nb; ++b) aRia += conj(ab[b]) * xb[b];
+        Pv = 1.0 / creal(aRia);
+        /* zpow analogue in beamspace: upper-triangle sum with w_bs */
+        for (int i = 0; i < Nb; ++i) {
+            cplx idot = 0;
+            for (int j = i; j < Nb; ++j) idot += conj(xb[j] / aRia) * Rb[i * Nb + j];
+            zp += idot * (xb[i] / aRia);
+        }
+    }
+
+    jb->z[pix] = zz;
+    if (jb->zpow) jb->zpow[pix] = zp;
+    if (jb->P) jb->P[pix] = Pv;
+    if (jb->w)
+        for (int i = 0; i < L; ++i) jb->w[pix * L + i] = wv[i];
+    if (jb->R)   /* loaded, normalised, full Hermitian, row-major per pixel */
+        for (int i = 0; i < L * L; ++i) jb->R[pix * L * L + i] = R[i];
+}
+
+static size_t scratch_elems(int M, int L, int Navg, int Nb)
+{
+    int T = 2 * Navg + 1;
+    size_t n = (size_t)T * M + (size_t)M * M + (size_t)L * L + 4 * (size_t)L + 2 * (size_t)L * L + L;
+    n += (size_t)Nb * L * 2 + (size_t)Nb * Nb * 3 + 4 * (size_t)Nb + 16;
+    return n;
+}
+
+static void *worker(void *arg)
+{
+    const job_t *jb = (const job_t *)arg;
+    cplx *scratch = (cplx *)malloc(sizeof(cplx) * scratch_elems(jb->M, jb->L, jb->Navg, jb->Nb));
+    if (!scratch) return (void *)1;
+    for (int x = jb->x0; x < jb->x1; ++x)
+        for (int y = jb->Navg; y < jb->Ny - jb->Navg; ++y) pixel_run(jb, x, y, scratch);
+    free(scratch);
+    return NULL;
+}
+
+/*
+ * Capon over a cube Xd[Nx][Ny][M] (interleaved complex64 input, as the GPU
+ * path receives it).  Outputs are complex128 / float64 arrays indexed
+ * [Nx][Ny-2*Navg](...).  `nthreads` splits the beams into contiguous slabs.
+ * Returns 0 on success, 1 on invalid arguments, 2 on allocation failure.
+ */
+int oracle_capon(const float *Xd, int Nx, int Ny, int M, double regCoef, int L, int Navg,
+                 int Nb, int bs_loading, int fp32_scalars,
+                 cplx *z, cplx *zpow, cplx *w, double *P, cplx *R, int nthreads)
+{
+    if (Nx < 1 || Ny < 1 || L < 1 || M < 1 || Navg < 0 || Nb < 0 || L > M || Nb > L ||
+        2 * Navg >= Ny || !Xd || !z)
+        return 1;
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > Nx) nthreads = Nx;
+    job_t base = {Xd, Nx, Ny, M, L, Navg, Nb, fp32_scalars, bs_loading, regCoef,
+                  z, zpow, w, R, P, 0, Nx};
+    if (nthreads == 1) return worker(&base) ? 2 : 0;
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * nthreads);
+    job_t *jobs = (job_t *)malloc(sizeof(job_t) * nthreads);
+    if (!th || !jobs) { free(th); free(jobs); return 2; }
+    int rc = 0;
+    for (int i = 0; i < nthreads; ++i) {
+        jobs[i] = base;
+        jobs[i].x0 = (int)((long)Nx * i / nthreads);
+        jobs[i].x1 = (int)((long)Nx * (i + 1) / nthreads);
+        pthread_create(&th[i], NULL, worker, &jobs[i]);
+    }
+    for (int i = 0; i < nthreads; ++i) {
+        void *ret = NULL;
+        pthread_join(th[i], &ret);
+        if (ret) rc = 2;
+    }
+    free(th);
+    free(jobs);
+    return rc;
+}

@@ -1,0 +1,227 @@
+"""Parity of the CUDA Capon path (through the C ABI) with the FP64 oracle and
+with outputs of the reference's own CPU path (golden fixtures).
+
+Error measures per pixel:
+  P: |P - P_ref| / P_ref                      (tolerance TOL_P, the FP32-path bar)
+  z: |z - z_ref| / sqrt(P_ref)                 (amplitude error on the output's own scale)
+  w: ||w - w_ref|| / ||w_ref||
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+TOL_P = 1e-4
+TOL_Z = 1e-3
+TOL_W = 2e-3
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+@pytest.fixture(scope="module")
+def cap():
+    from cos_gb300 import capon
+    return capon
+
+
+def errors(z, P, w, ref):
+    e = {"P": np.abs(P - ref["P"]) / ref["P"],
+         "z": np.abs(z - ref["z"]) / np.sqrt(ref["P"])}
+    if w is not None and ref.get("w") is not None:
+        e["w"] = np.linalg.norm(w - ref["w"], axis=-1) / np.linalg.norm(ref["w"], axis=-1)
+    return e
+
+
+def assert_close(z, P, w, ref, tol_p=TOL_P, tol_z=TOL_Z, tol_w=TOL_W, what=""):
+    e = errors(z, P, w, ref)
+    msg = f"{what}: " + ", ".join(f"{k} max {v.max():.2e} med {np.median(v):.2e}" for k, v in e.items())
+    print(msg)
+    assert np.all(np.isfinite(z)) and np.all(np.isfinite(P)), msg
+    assert e["P"].max() <= tol_p, msg
+    assert e["z"].max() <= tol_z, msg
+    if "w" in e:
+        assert e["w"].max() <= tol_w, msg
+
+
+@pytest.mark.parametrize("form", [0, 1])
+def test_config0_slice(cap, form):
+    from cos_gb300 import synth
+    c = synth.config0(seed=0)
+    x = np.ascontiguousarray(c["x"][:16])
+    z, P, w = cap.getCaponGPU(x, c["d"], c["L"], c["K"], form=form)
+    ref = oracle.capon(x, c["d"], c["L"], c["K"], nthreads=8)
+    assert_close(z, P, w, ref, what=f"config0 form{form}")
+
+
+@pytest.mark.parametrize("form", [0, 1])
+def test_config1_slice(cap, form):
+    from cos_gb300 import synth
+    c = synth.config1(seed=1, Nx=8)
+    x = c["x"]
+    z, P, w = cap.getCaponGPU(x, c["d"], c["L"], c["K"], form=form)
+    ref = oracle.capon(x, c["d"], c["L"], c["K"], nthreads=8)
+    assert_close(z, P, w, ref, what=f"config1 form{form}")
+
+
+@pytest.mark.parametrize("form", [0, 1])
+def test_reference_golden_cases(cap, form):
+    """z and w against the reference CPU path's own outputs."""
+    g = np.load(os.path.join(GOLD, "capon_ref_cases.npz"))
+    for i, (Nx, Ny, M, L, K, d, _seed) in enumerate(g["cases"]):
+        x = g[f"x{i}"]
+        z, P, w = cap.getCaponGPU(x, d, int(L), int(K), form=form)
+        ref = oracle.capon(x, d, int(L), int(K))
+        np.testing.assert_allclose(ref["z"], g[f"z{i}"], rtol=1e-10, atol=1e-12)
+        assert_close(z, P, w, dict(ref, z=g[f"z{i}"], w=g[f"w{i}"]), what=f"golden case {i} form{form}")
+
+
+@pytest.mark.parametrize("bs_loading", [0, 1])
+@pytest.mark.parametrize("M,L,Nb", [(96, 48, 3), (128, 64, 5), (32, 16, 4), (24, 12, 7)])
+def test_beamspace(cap, M, L, Nb, bs_loading):
+    from cos_gb300 import synth
+    x = synth.cube(96, 6, M, [10.0, 5.0], seed=M + Nb)
+    V = np.zeros((Nb, L))
+    z, P, w = cap.getCaponGPU(x, 0.01, L, 1, V, loading=bs_loading)
+    ref = oracle.capon(x, 0.01, L, 1, Nb=Nb, bs_loading=bool(bs_loading), nthreads=6)
+    assert_close(z, P, w, ref, what=f"beamspace M{M} L{L} Nb{Nb} load{bs_loading}")
+
+
+def test_beamspace_full_dft_equals_element_space(cap):
+    from cos_gb300 import synth
+    x = synth.cube(64, 4, 24, [10.0], seed=5)
+    V = np.zeros((11, 11))
+    zb, Pb, wb = cap.getCaponGPU(x, 0.05, 11, 1, V)
+    ref = oracle.capon(x, 0.05, 11, 1)
+    assert_close(zb, Pb, wb, ref, what="beamspace Nb=L")
+
+
+def test_drop_in_getCaponCUDAPy(cap):
+    """[z, R, w, e] with R as the reference GPU writes it: per pixel
+    column-major, loaded, not normalised (buildR_kernel.cu:84-86, 153-157)."""
+    from cos_gb300 import synth
+    c = synth.config0(seed=4)
+    x = np.ascontiguousarray(c["x"][:2, :64])
+    z, R, w, e = cap.getCaponCUDAPy(x, c["d"], c["L"], c["K"], np.array([0]), False, False)
+    assert e == 0
+    ref = oracle.capon(x, c["d"], c["L"], c["K"], want_R=True)
+    Ns, T = x.shape[2] - c["L"] + 1, 2 * c["K"] + 1
+    R_expect = np.swapaxes(ref["R"], -1, -2) * (Ns * T)   # column-major memory of R_true
+    err = np.abs(R - R_expect).max() / np.abs(R_expect).max()
+    assert err < 1e-5, err
+    assert_close(z, ref["P"], w, ref, what="getCaponCUDAPy")
+
+
+@pytest.mark.parametrize("form", [0, 1])
+def test_normalised_R_output(cap, form):
+    from cos_gb300 import _lib
+    rng = np.random.default_rng(3)
+    x = (rng.standard_normal((2, 30, 32)) + 1j * rng.standard_normal((2, 30, 32))).astype(np.complex64)
+    ctx = cap.Capon()
+    L, K = 16, 2
+    npy = 30 - 2 * K
+    z = np.zeros((2, npy), np.complex64)
+    P = np.zeros((2, npy), np.float32)
+    R = np.zeros((2, npy, L, L), np.complex64)
+    rc = ctx.getCaponEx(z, P, None, R, x, 0.01, L, K, 32, 2, 30, 0,
+                        cap.opts(form=form, r_layout=_lib.R_NORMALISED))
+    assert rc == 0
+    ref = oracle.capon(x, 0.01, L, K, want_R=True)
+    assert np.abs(R - ref["R"]).max() / np.abs(ref["R"]).max() < 1e-5
+
+
+def test_build_r_entry_point(cap):
+    rng = np.random.default_rng(11)
+    Nx, Nz, M, L, K = 2, 20, 24, 10, 1
+    x = (rng.standard_normal((Nx, Nz, M)) + 1j * rng.standard_normal((Nx, Nz, M))).astype(np.complex64)
+    R = np.zeros((Nx, Nz - 2 * K, L, L), np.complex64)
+    assert cap.BuildR().getR(R, x, 0.02, L, K, M, Nx, Nz, 0) == 0
+    ref = oracle.capon(x, 0.02, L, K, want_R=True)
+    expect = np.swapaxes(ref["R"], -1, -2) * ((M - L + 1) * (2 * K + 1))
+    assert np.abs(R - expect).max() / np.abs(expect).max() < 1e-5
+
+
+def test_solver_entry_point_general_matrices(cap):
+    """testRTC.pyx:183-236: general complex systems, A column-major."""
+    rng = np.random.default_rng(12)
+    for N, batch in ((3, 2), (16, 50), (72, 7)):
+        A = (rng.standard_normal((batch, N, N)) + 1j * rng.standard_normal((batch, N, N))).astype(np.complex64)
+        A += (10 * np.eye(N)).astype(np.complex64)
+        b = (rng.standard_normal((batch, N)) + 1j * rng.standard_normal((batch, N))).astype(np.complex64)
+        x = np.zeros((batch, N), np.complex64)
+        assert cap.Solver().solve(x, A, b, N, batch) == 0
+        xr = np.stack([np.linalg.solve(A[i].T.astype(np.complex128), b[i]) for i in range(batch)])
+        assert np.abs(x - xr).max() / np.abs(xr).max() < 1e-4
+
+
+def test_solver_known_answers(cap):
+    ka = np.load(os.path.join(GOLD, "linalg_known_answers.npz"))
+    for A, b, xe in ((ka["A"], ka["b1"], ka["x1"]), (ka["A"], ka["b2"], ka["x2"]),
+                     (ka["complexA"], ka["complexb"], ka["complexx"])):
+        Acm = np.ascontiguousarray(A.T[None].astype(np.complex64))   # column-major memory
+        x = np.zeros((1, 3), np.complex64)
+        assert cap.Solver().solve(x, Acm, b[None].astype(np.complex64), 3, 1) == 0
+        np.testing.assert_allclose(x[0], xe, rtol=1e-5, atol=1e-6)
+
+
+def test_butler_entry_point(cap):
+    for Nb, L in ((3, 3), (5, 64), (3, 48), (4, 9)):
+        np.testing.assert_allclose(cap.butler_matrix(Nb, L), oracle.butler(Nb, L), atol=2e-7)
+
+
+@pytest.mark.parametrize("args,code", [
+    (dict(L=0), 719), (dict(M=0), 719), (dict(Nx=0), 719), (dict(K=-1), 719), (dict(Nb=-1), 719),
+    (dict(Nb=9), 719), (dict(L=40), 719), (dict(K=10), 719), (dict(L=65, M=80), 801),
+])
+def test_invalid_sizes_return_reference_codes(cap, args, code):
+    """Capon.cpp:98-107 / BuildR.cpp:37-48 return cudaErrorLaunchFailure (719)."""
+    a = dict(L=8, K=1, M=32, Nx=2, Nz=20, Nb=0)
+    a.update(args)
+    Mx = max(a["M"], 1)
+    x = np.zeros((2, 20, Mx), np.complex64)
+    z = np.zeros(4096, np.complex64)
+    w = np.zeros(4096 * 8, np.complex64)
+    rc = cap.Capon().getCapon(z, w, None, x, 0.01, a["L"], a["K"], a["M"], a["Nx"], a["Nz"], a["Nb"])
+    assert rc == code
+
+
+def test_multi_frame_single_call(cap):
+    """Frames of different M, L, Nb in one cos_capon_run call (config-2 shapes, fewer beams)."""
+    import torch
+    from cos_gb300 import synth
+    frames, refs = [], []
+    for fr in synth.config2(seed=2, Ny=96, Nx=4):
+        xt = torch.from_numpy(fr["x"]).cuda()
+        Nx, Ny, M = fr["x"].shape
+        npy = Ny - 2 * fr["K"]
+        f = cap.DeviceFrame(x=xt, L=fr["L"], K=fr["K"], d=fr["d"], Nb=fr["Nb"],
+                            P=torch.empty((Nx, npy), dtype=torch.float32, device="cuda"),
+                            w=torch.empty((Nx, npy, fr["L"]), dtype=torch.complex64, device="cuda"))
+        frames.append(f)
+        refs.append(oracle.capon(fr["x"], fr["d"], fr["L"], fr["K"], Nb=fr["Nb"], nthreads=4))
+    cap.capon_frames(frames)
+    torch.cuda.synchronize()
+    for f, ref in zip(frames, refs):
+        assert_close(f.z.cpu().numpy(), f.P.cpu().numpy(), f.w.cpu().numpy(), ref,
+                     what=f"multi-frame L{f.L} Nb{f.Nb}")
+
+
+def test_full_size_config1_properties(cap):
+    """Config-1 size (523,264 pixels): deterministic reruns, positive finite
+    power, fused == plain within tolerance, and oracle parity on sampled beams."""
+    from cos_gb300 import synth
+    c = synth.config1(seed=1)
+    x = c["x"]
+    z1, P1, w1 = cap.getCaponGPU(x, c["d"], c["L"], c["K"], want_w=False)
+    z2, P2, _ = cap.getCaponGPU(x, c["d"], c["L"], c["K"], want_w=False)
+    np.testing.assert_array_equal(z1, z2)
+    np.testing.assert_array_equal(P1, P2)
+    assert np.all(np.isfinite(z1)) and np.all(P1 > 0)
+    zp, Pp, _ = cap.getCaponGPU(x, c["d"], c["L"], c["K"], form=1, want_w=False)
+    assert np.max(np.abs(Pp - P1) / P1) < 2 * TOL_P
+    beams = [0, 97, 255]
+    sub = np.ascontiguousarray(x[beams])
+    ref = oracle.capon(sub, c["d"], c["L"], c["K"], want_w=False, nthreads=3)
+    assert_close(z1[beams], P1[beams], None, ref, what="config1 full-size sampled beams")

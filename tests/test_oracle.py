@@ -1,0 +1,150 @@
+"""The FP64 oracle pinned against the reference: its linear-algebra known
+answers (framework/linalg/tests) and outputs of the reference's own CPU Capon
+path (getCaponC.getCaponCPy) on seeded inputs.  CPU only."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+KA = np.load(os.path.join(GOLD, "linalg_known_answers.npz"))
+CASES = np.load(os.path.join(GOLD, "capon_ref_cases.npz"))
+
+
+def test_cholesky_known_answers():
+    # testCholesky.py:16-23 (real tridiagonal) and :61-68 (complex Hermitian), 14 places
+    np.testing.assert_allclose(oracle.cholesky(KA["A"]), KA["R"], atol=1e-14)
+    np.testing.assert_allclose(oracle.cholesky(KA["complexA"]), KA["complexR"], atol=1e-14)
+    U = oracle.cholesky(KA["complexA"])
+    np.testing.assert_allclose(U.conj().T @ U, KA["complexA"], atol=1e-13)
+
+
+def test_triangular_solves_known_answers():
+    # testCholesky.py:40-58 and :70-82; testLinearSolvec.py:145-154
+    U = oracle.cholesky(KA["A"])
+    for b, x in (("b1", "x1"), ("b2", "x2")):
+        y = oracle.forward_solve(U.conj().T, KA[b])
+        np.testing.assert_allclose(oracle.back_solve(U, y), KA[x], atol=1e-14)
+    U = oracle.cholesky(KA["complexA"])
+    y = oracle.forward_solve(U.conj().T, KA["complexb"])
+    np.testing.assert_allclose(y, KA["complexy"], atol=1e-14)
+    np.testing.assert_allclose(oracle.back_solve(U, y), KA["complexx"], atol=1e-14)
+    np.testing.assert_array_equal(oracle.back_solve(KA["C"], KA["b1c"]), KA["x1c"])
+    np.testing.assert_array_equal(oracle.forward_solve(KA["C"].conj().T, KA["b1c"]), KA["x1cT"])
+
+
+def test_solve_cholesky_known_answers():
+    # testLinearSolvec.py:119-129
+    np.testing.assert_allclose(oracle.solve_cholesky(KA["A"], KA["b1"]), KA["x1"], atol=1e-14)
+    np.testing.assert_allclose(oracle.solve_cholesky(KA["complexA"], KA["complexb"]), KA["complexx"], atol=1e-14)
+    rng = np.random.default_rng(5)
+    L = 24
+    U = np.triu(rng.standard_normal((L, L)) + 1j * rng.standard_normal((L, L))) + np.eye(L) * 100
+    A = U.conj().T @ U
+    b = rng.standard_normal(L) + 1j * rng.standard_normal(L)
+    np.testing.assert_allclose(oracle.solve_cholesky(A, b), np.linalg.solve(A, b), rtol=1e-12, atol=1e-15)
+
+
+def test_butler_known_answers():
+    # testBeamspace.py:14-29 (first-Nb-bins layout of beamspace.butlerMatrix)
+    np.testing.assert_allclose(oracle.butler(4, 4, symmetric=False), KA["but4"], atol=1e-15)
+    np.testing.assert_allclose(oracle.butler(3, 3, symmetric=False), KA["but3"], atol=1e-15)
+    np.testing.assert_allclose(oracle.butler(2, 3, symmetric=False) @ KA["complexb"], KA["bsComplexb"], atol=1e-14)
+    # the GPU layout agrees with it whenever Nb is odd or Nb < L ... for these sizes
+    np.testing.assert_allclose(oracle.butler(3, 3), KA["but3"], atol=1e-15)
+    np.testing.assert_allclose(oracle.butler(2, 3) @ KA["complexb"], KA["bsComplexb"], atol=1e-14)
+
+
+def test_butler_gpu_layout_bins():
+    # capon_kernel.cu:53-59: beams above Nb/2 take the negative bins
+    B = oracle.butler(5, 64)
+    bins = np.round(np.angle(B[:, 1]) / (-2 * np.pi / 64)).astype(int) % 64
+    assert list(bins) == [0, 1, 2, 62, 63]
+    np.testing.assert_allclose(B @ B.conj().T, np.eye(5), atol=1e-14)
+
+
+@pytest.mark.parametrize("i", range(len(CASES["cases"])))
+def test_oracle_matches_reference_cpu_path(i):
+    Nx, Ny, M, L, K, d, _seed = CASES["cases"][i]
+    x = CASES[f"x{i}"]
+    o = oracle.capon(x, d, int(L), int(K))
+    zr, zpr, wr = CASES[f"z{i}"], CASES[f"zpow{i}"], CASES[f"w{i}"]
+    assert o["z"].shape == zr.shape and o["w"].shape == wr.shape
+    np.testing.assert_allclose(o["z"], zr, rtol=1e-10, atol=1e-12 * np.abs(zr).max())
+    np.testing.assert_allclose(o["zpow"], zpr, rtol=1e-10, atol=1e-12 * np.abs(zpr).max())
+    np.testing.assert_allclose(o["w"], wr, rtol=1e-9, atol=1e-11 * np.abs(wr).max())
+
+
+def test_power_definitions():
+    """P = w^H R_d w = 1/Re(a^H R_d^-1 a); the reference's zPow satisfies
+    2 Re(zPow) - sum_i R_ii |w_i|^2 = w^H conj(R_d) w (upper-triangle sum of
+    w_i R_ij conj(w_j))."""
+    i = 0
+    Nx, Ny, M, L, K, d, _ = CASES["cases"][i]
+    o = oracle.capon(CASES[f"x{i}"], d, int(L), int(K), want_R=True)
+    R, w = o["R"], o["w"]
+    np.testing.assert_allclose(np.einsum("xyi,xyij,xyj->xy", w.conj(), R, w).real, o["P"], rtol=1e-12)
+    lhs = 2 * CASES[f"zpow{i}"].real - np.einsum("xyii,xyi->xy", R, np.abs(w) ** 2).real
+    rhs = np.einsum("xyi,xyij,xyj->xy", w.conj(), R.conj(), w).real
+    np.testing.assert_allclose(lhs, rhs, rtol=1e-10)
+
+
+def test_oracle_threads_identical():
+    x = CASES["x0"]
+    a = oracle.capon(x, 0.01, 16, 1, nthreads=1)
+    b = oracle.capon(x, 0.01, 16, 1, nthreads=3)
+    for k in ("z", "zpow", "P", "w"):
+        np.testing.assert_array_equal(a[k], b[k])
+
+
+def test_beamspace_full_dft_equals_element_space():
+    # with Nb = L (odd) the Butler matrix is unitary, so beamspace Capon with
+    # either loading convention reproduces element-space Capon exactly
+    rng = np.random.default_rng(7)
+    x = (rng.standard_normal((2, 14, 12)) + 1j * rng.standard_normal((2, 14, 12))).astype(np.complex64)
+    e = oracle.capon(x, 0.05, 5, 1)
+    for bsl in (False, True):
+        b = oracle.capon(x, 0.05, 5, 1, Nb=5, bs_loading=bsl)
+        np.testing.assert_allclose(b["z"], e["z"], rtol=1e-9, atol=1e-12)
+        np.testing.assert_allclose(b["P"], e["P"], rtol=1e-9)
+        np.testing.assert_allclose(b["w"], e["w"], rtol=1e-9, atol=1e-12)
+
+
+def test_beamspace_reduces_dimension():
+    rng = np.random.default_rng(8)
+    x = (rng.standard_normal((2, 12, 16)) + 1j * rng.standard_normal((2, 12, 16))).astype(np.complex64)
+    b = oracle.capon(x, 0.01, 8, 1, Nb=3)
+    # w lies in the span of the Butler rows: w = B^H w_bs
+    B = oracle.butler(3, 8)
+    w = b["w"].reshape(-1, 8)
+    proj = w @ B.conj().T @ B
+    np.testing.assert_allclose(proj, w, atol=1e-12)
+    assert np.all(b["P"] > 0)
+
+
+@pytest.mark.parametrize("bad", [
+    dict(L=0), dict(L=20), dict(K=-1), dict(K=6), dict(Nb=9), dict(Nb=-1),
+])
+def test_oracle_rejects_invalid_sizes(bad):
+    args = dict(L=8, K=1, Nb=0)
+    args.update(bad)
+    x = np.zeros((2, 12, 16), np.complex64)
+    with pytest.raises(ValueError):
+        oracle.capon(x, 0.01, args["L"], args["K"], Nb=args["Nb"])
+
+
+def test_reference_cpu_path_live():
+    """When the reference's compiled CPU path is present, re-run it on a fresh
+    seeded case (beyond the committed fixtures)."""
+    import ref
+    if not ref.available():
+        pytest.skip("reference CPU path not built here")
+    g = ref.load()
+    rng = np.random.default_rng(99)
+    x = (rng.standard_normal((2, 22, 20)) + 1j * rng.standard_normal((2, 22, 20))).astype(np.complex64)
+    zr, zpr, wr = g.getCaponCPy(x.astype(np.complex128), 0.02, 7, 2, np.array([]), False, False)
+    o = oracle.capon(x, 0.02, 7, 2)
+    np.testing.assert_allclose(o["z"], zr, rtol=1e-10, atol=1e-13)
+    np.testing.assert_allclose(o["w"], wr, rtol=1e-9, atol=1e-12)
