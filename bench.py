@@ -328,6 +328,22 @@ def run_gpu(args) -> None:
         dist.destroy_process_group()
 
 
+def run_profile_case(args) -> None:
+    """The fused kernel alone on Nx=profile_nx beams (for ncu captures)."""
+    import torch
+    from cos_gb300 import _lib, capon, synth
+    x = synth.config1(seed=1, Nx=args.profile_nx)["x"]
+    xt = torch.from_numpy(x).cuda()
+    f = capon.DeviceFrame(x=xt, L=L, K=K, d=D,
+                          z=torch.empty((args.profile_nx, NY - 2 * K), dtype=torch.complex64, device="cuda"),
+                          P=torch.empty((args.profile_nx, NY - 2 * K), dtype=torch.float32, device="cuda"))
+    ctx = capon.Context()
+    for _ in range(args.warmup + args.steps):
+        capon.capon_frames([f], ctx, capon.opts(form=_lib.FORM_FUSED))
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": {"Nx": args.profile_nx, "launches": args.warmup + args.steps}}))
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -335,8 +351,12 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-nx", type=int, default=0,
+                    help="profiling case: only the fused kernel, warmup+steps launches on Nx beams of the workload")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.profile_nx:
+        run_profile_case(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)

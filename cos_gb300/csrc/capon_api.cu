@@ -7,11 +7,14 @@
 // synchronisation between stages, and keeps covariance matrices on chip.
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
+#include <map>
 #include <new>
+#include <tuple>
 #include <vector>
 
 #include "capon_internal.h"
@@ -54,6 +57,9 @@ struct cos_capon_ctx {
     DevBuf Rwork, Ria;
     // stage entry points
     DevBuf A, b, sol;
+    // autotuner: chosen fused candidate per (L, K, M, w-or-R requested)
+    std::map<std::tuple<int, int, int, int>, int> tuned;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
 
 static const cos_capon_opts kDefaultOpts = {COS_CAPON_FORM_FUSED, COS_CAPON_LOAD_ELEMENT, COS_CAPON_R_REFERENCE, 0};
@@ -105,9 +111,96 @@ static FrameDev make_frame(const cos_capon_frame &fr, const cos_capon_opts &o)
     return f;
 }
 
+static int candidates(int L, int K, const FusedCandidate **out)
+{
+    *out = nullptr;
+    const int T = 2 * K + 1;
+    if (L == 16 && T == 1) return fused_candidates_l16_t1(out);
+    if (L == 16 && T == 3) return fused_candidates_l16_t3(out);
+    if (L == 16 && T == 5) return fused_candidates_l16_t5(out);
+    if (L == 32 && T == 1) return fused_candidates_l32_t1(out);
+    if (L == 32 && T == 3) return fused_candidates_l32_t3(out);
+    if (L == 32 && T == 5) return fused_candidates_l32_t5(out);
+    return 0;
+}
+
 static bool use_fused(const FrameDev &f, const cos_capon_opts &o)
 {
-    return o.form == COS_CAPON_FORM_FUSED && f.Nb == 0 && fused_supported(f.L) && 2 * f.K + 1 <= fused_tmax(f.L);
+    if (o.form != COS_CAPON_FORM_FUSED || f.Nb != 0) return false;
+    const FusedCandidate *c = nullptr;
+    const int n = candidates(f.L, f.K, &c);
+    for (int i = 0; i < n; ++i)
+        if (c[i].M == 0 || c[i].M == f.M) return true;
+    return false;
+}
+
+// Autotuner: the first launch of an (L, K, M, w/R) shape on a context times
+// every candidate configuration on the frames themselves (each candidate
+// computes the same per-pixel arithmetic), keeps the fastest, and reruns it so
+// that the outputs are the winner's.  COS_CAPON_FUSED_CONFIG=<name> forces a
+// candidate.  While the stream is being captured into a graph no timing is
+// possible, so an untuned shape then takes the first candidate.
+static int launch_fused_tuned(cos_capon_ctx *c, const FramesParam &fp, bool wr, cudaStream_t s)
+{
+    const FrameDev &f0 = fp.f[0];
+    const FusedCandidate *cand = nullptr;
+    const int n = candidates(f0.L, f0.K, &cand);
+    std::vector<int> ok;
+    for (int i = 0; i < n; ++i) {
+        bool fits = cand[i].M == 0;
+        if (!fits) {
+            fits = true;
+            for (int q = 0; q < fp.n; ++q) fits &= (fp.f[q].M == cand[i].M);
+        }
+        if (fits) ok.push_back(i);
+    }
+    if (ok.empty()) return COS_CAPON_ERR_NOT_SUPPORTED;
+    if (const char *force = getenv("COS_CAPON_FUSED_CONFIG")) {
+        for (int i : ok)
+            if (!strcmp(force, cand[i].name)) return cand[i].launch(fp, wr, c->d_status, c->num_sms, s);
+    }
+    const auto key = std::make_tuple(f0.L, f0.K, f0.M, (int)wr);
+    auto it = c->tuned.find(key);
+    if (it != c->tuned.end()) return cand[it->second].launch(fp, wr, c->d_status, c->num_sms, s);
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone || ok.size() == 1)
+        return cand[ok[0]].launch(fp, wr, c->d_status, c->num_sms, s);
+    if (!c->ev0) {
+        if (cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) {
+            cudaGetLastError();
+            return cand[ok[0]].launch(fp, wr, c->d_status, c->num_sms, s);
+        }
+    }
+    int best = ok[0];
+    float best_ms = 1e30f;
+    for (int i : ok) {
+        // one untimed launch, then the best of two timed ones
+        int e = cand[i].launch(fp, wr, c->d_status, c->num_sms, s);
+        if (e == cudaErrorNotSupported) {
+            cudaGetLastError();
+            continue;
+        }
+        if (e) return e;
+        float ms = 1e30f;
+        for (int rep = 0; rep < 2; ++rep) {
+            cudaEventRecord(c->ev0, s);
+            if ((e = cand[i].launch(fp, wr, c->d_status, c->num_sms, s))) return e;
+            cudaEventRecord(c->ev1, s);
+            if (cudaEventSynchronize(c->ev1) != cudaSuccess) return cudaGetLastError();
+            float t = 0.f;
+            cudaEventElapsedTime(&t, c->ev0, c->ev1);
+            ms = t < ms ? t : ms;
+        }
+        if (getenv("COS_CAPON_TUNE_VERBOSE")) fprintf(stderr, "[cos_capon] tune %s: %.3f ms\n", cand[i].name, ms);
+        if (ms < best_ms) {
+            best_ms = ms;
+            best = i;
+        }
+    }
+    c->tuned[key] = best;
+    if (getenv("COS_CAPON_TUNE_VERBOSE")) fprintf(stderr, "[cos_capon] L=%d K=%d M=%d wr=%d -> %s (%.3f ms)\n",
+                                                  f0.L, f0.K, f0.M, (int)wr, cand[best].name, best_ms);
+    return cand[best].launch(fp, wr, c->d_status, c->num_sms, s);
 }
 
 // plain three-stage pipeline for one element-space frame
@@ -137,19 +230,15 @@ static int run_frames(cos_capon_ctx *c, const FrameDev *fs, int n, const cos_cap
         if (use_fused(f, o)) {
             FramesParam fp;
             memset(&fp, 0, sizeof(fp));
-            long long begin = 0;
+            bool wr = false;
             int j = i;
             while (j < n && fp.n < kMaxFrames && use_fused(fs[j], o) && fs[j].L == f.L && fs[j].K == f.K &&
                    fs[j].M == f.M) {
-                FrameDev g = fs[j];
-                g.tile = fused_tile(g.L);
-                g.tiles_per_beam = (g.Npy + g.tile - 1) / g.tile;
-                g.tile_begin = begin;
-                begin += (long long)g.Nx * g.tiles_per_beam;
-                fp.f[fp.n++] = g;
+                wr |= (fs[j].w != nullptr) || (fs[j].R != nullptr);
+                fp.f[fp.n++] = fs[j];
                 ++j;
             }
-            int e = launch_fused_frames(fp, c->d_status, c->num_sms, s);
+            int e = launch_fused_tuned(c, fp, wr, s);
             if (e) return e;
             i = j;
         } else if (f.Nb > 0) {
@@ -217,6 +306,8 @@ int cos_capon_destroy(cos_capon_ctx *c)
     for (DevBuf *b : {&c->x, &c->z, &c->P, &c->w, &c->R, &c->Rwork, &c->Ria, &c->A, &c->b, &c->sol}) b->release();
     if (c->d_status) cudaFree(c->d_status);
     if (c->stream) cudaStreamDestroy(c->stream);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
     delete c;
     return 0;
 }
@@ -252,7 +343,13 @@ int cos_capon_get_capon_ex(cos_capon_ctx *c, void *z, float *P, void *w, void *R
     const size_t N = (size_t)Nx * Nz, npix = (size_t)Nx * (Nz - 2 * Yavg);
     const size_t bx = N * M * sizeof(float2), bz = npix * sizeof(float2), bp = npix * sizeof(float),
                  bw = npix * L * sizeof(float2), bR = npix * L * L * sizeof(float2);
-    const bool plain = !(o.form == COS_CAPON_FORM_FUSED && Nb == 0 && fused_supported(L));
+    cos_capon_frame probe;
+    memset(&probe, 0, sizeof(probe));
+    probe.L = L;
+    probe.K = Yavg;
+    probe.M = M;
+    probe.Nb = Nb;
+    const bool plain = !use_fused(make_frame(probe, o), o);
     size_t need = 0;
     need += bx > c->x.cap ? bx : 0;
     need += bz > c->z.cap ? bz : 0;

@@ -115,10 +115,18 @@ beamspace_kernel(FrameDev f, float2 *__restrict__ Rbs)
         int bb = 0, rem = e;
         while (rem >= Nb - bb) { rem -= Nb - bb; ++bb; }
         const int cc = bb + rem;
-        float2 acc = make_float2(0.f, 0.f);
-        for (int q = 0; q < T * Ns; ++q) acc = cadd(acc, cmulc(Y[(size_t)q * Nb + bb], Y[(size_t)q * Nb + cc]));
-        Cm[bb * S.ld + cc] = acc;
-        Cm[cc * S.ld + bb] = cconj(acc);
+        // chunks of 4 products summed in FP32, chunk sums accumulated in
+        // float-float (TwoSum): one rounding for the whole T*Ns-term sum
+        float2 hi = make_float2(0.f, 0.f), lo = make_float2(0.f, 0.f);
+        for (int q0 = 0; q0 < T * Ns; q0 += 4) {
+            float2 acc = make_float2(0.f, 0.f);
+            const int q1 = min(T * Ns, q0 + 4);
+            for (int q = q0; q < q1; ++q) acc = cadd(acc, cmulc(Y[(size_t)q * Nb + bb], Y[(size_t)q * Nb + cc]));
+            two_sum_acc(hi, lo, acc);
+        }
+        const float2 v = fadd2(hi, lo);
+        Cm[bb * S.ld + cc] = v;
+        Cm[cc * S.ld + bb] = cconj(v);
     }
     __syncwarp();
     if (lane == 0) {

@@ -67,6 +67,17 @@ COS_DEV float2 cnmac_conj(float2 acc, float2 nu1, float2 nu2, float2 v)
     return ffma2(nu2, make_float2(v.y, v.x), acc);
 }
 
+// float-float accumulation of complex values: (hi, lo) += v exactly up to the
+// rounding of lo (Knuth's TwoSum on both components, packed).
+COS_DEV void two_sum_acc(float2 &hi, float2 &lo, float2 v)
+{
+    const float2 s = fadd2(hi, v);
+    const float2 bb = fsub2(s, hi);
+    const float2 e = fadd2(fsub2(hi, fsub2(s, bb)), fsub2(v, bb));
+    hi = s;
+    lo = fadd2(lo, e);
+}
+
 // ---- warp helpers ---------------------------------------------------------
 COS_DEV float2 shfl2(float2 v, int src, int width)
 {

@@ -24,11 +24,13 @@
 //      and, when asked, w = U^-1 y1 / |y1|^2 by back substitution
 //      (linearSolvec.pyx:330-346).
 // Arithmetic is FP32 with packed fma.rn.f32x2.
+#pragma once
 #include "capon_common.cuh"
 #include "capon_internal.h"
 #include "../../include/cos_capon.h"
 
 namespace cgb {
+namespace fused {
 
 // ---- mbarrier / bulk-copy primitives ---------------------------------------
 COS_DEV uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -71,9 +73,17 @@ COS_DEV void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;"
 COS_DEV void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
 
 // ---- compile-time configuration --------------------------------------------
-template <int L_, int G_, int WARPS_, int NITER_, int TMAX_>
+// L: subarray length; G: lanes per pixel (lane r owns columns j = m*G + r);
+// WARPS x NITER x (32/G) pixels per tile; T: the temporal window 2K+1 (exact,
+// so the window loops carry no runtime bound); M: channel count, 0 = taken at
+// run time (a compile-time M turns every shared-memory offset of the unrolled
+// code into an immediate); SYNC: barrier points that keep the CTA's warps in
+// step, so that the long unrolled instruction stream is fetched once for all
+// of them.
+template <int L_, int G_, int WARPS_, int NITER_, int T_, int M_, bool SYNC_>
 struct Cfg {
-    static constexpr int L = L_, G = G_, WARPS = WARPS_, NITER = NITER_, TMAX = TMAX_;
+    static constexpr int L = L_, G = G_, WARPS = WARPS_, NITER = NITER_, T = T_, M = M_;
+    static constexpr bool SYNC = SYNC_;
     static constexpr int NM = L / G;       // column slots per lane
     static constexpr int PPW = 32 / G;     // pixels per warp
     static constexpr int TILE = WARPS * PPW * NITER;
@@ -93,7 +103,7 @@ struct Smem {
         off_raw1 = off_raw0 + raw;
         off_xe = off_raw1 + raw;
         off_c = off_xe + (((size_t)rows * XS * sizeof(float4) + 127) & ~(size_t)127);
-        off_g = off_c + (((size_t)rows * L * sizeof(float2) + 127) & ~(size_t)127);
+        off_g = off_c + (((size_t)2 * rows * L * sizeof(float2) + 127) & ~(size_t)127);
         off_rb = off_g + (((size_t)TILE * L * sizeof(float2) + 127) & ~(size_t)127);
         off_bar = off_rb + (((size_t)WARPS * PPW * (L + 1) * sizeof(float4) + 127) & ~(size_t)127);
         total = off_bar + 64;
@@ -108,11 +118,13 @@ COS_DEV int unit_frame(const FramesParam &fp, long long u)
     return f;
 }
 
-template <class C>
+// WR: the instantiation that can also write w and R; the z/P-only one omits
+// that code so its instruction footprint stays smaller.
+template <class C, bool WR>
 __global__ void __launch_bounds__(C::WARPS * 32, 1)
 fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsigned *status)
 {
-    constexpr int L = C::L, G = C::G, NM = C::NM, PPW = C::PPW, TILE = C::TILE, TMAX = C::TMAX;
+    constexpr int L = C::L, G = C::G, NM = C::NM, PPW = C::PPW, TILE = C::TILE, T = C::T, K = (C::T - 1) / 2;
     extern __shared__ __align__(128) unsigned char smem[];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int gi = lane / G, r = lane % G;
@@ -121,10 +133,11 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
     // all frames of one launch share K and M bounds through the first frame's
     // carve-up; the host groups frames so that K and M are equal within a launch
     const FrameDev &f0 = fp.f[0];
-    const Smem S(TILE, f0.K, f0.M, L, C::WARPS, PPW);
+    const Smem S(TILE, K, C::M ? C::M : f0.M, L, C::WARPS, PPW);
     float2 *raw[2] = {(float2 *)(smem + S.off_raw0), (float2 *)(smem + S.off_raw1)};
     float4 *xe = (float4 *)(smem + S.off_xe);
     float2 *cs = (float2 *)(smem + S.off_c);
+    float2 *cl = cs + (size_t)S.rows * L;
     float2 *gs = (float2 *)(smem + S.off_g);
     float4 *rb = (float4 *)(smem + S.off_rb) + (size_t)(warp * PPW + gi) * (L + 1);
     uint64_t *bar = (uint64_t *)(smem + S.off_bar);
@@ -164,7 +177,7 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
         if (tid == 0 && un < total_units) issue(un, b ^ 1);
 
         const FrameDev &f = fp.f[unit_frame(fp, u)];
-        const int M = f.M, K = f.K, T = 2 * K + 1, Ns = M - L + 1;
+        const int M = C::M ? C::M : f.M, Ns = M - L + 1;
         const long long lu = u - f.tile_begin;
         const int bx = (int)(lu / f.tiles_per_beam);
         const int p0 = (int)(lu % f.tiles_per_beam) * TILE;
@@ -187,30 +200,63 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
             xe[rr * XS + cc] = make_float4(v.x, v.y, v.y, -v.x);
         }
         __syncthreads();
-        for (int i = tid; i < rows * L; i += nthreads) {
-            const int rr = i / L, j = i % L;
+        // c_y[j] for 4 consecutive j per thread (the window x[s+j..s+j+3] slides
+        // through registers, one new load per term): packed FP32 products summed
+        // in chunks of 4 terms, chunk sums accumulated in float-float (TwoSum),
+        // so the first covariance row -- which every diagonal of R starts from --
+        // carries one rounding only
+        static_assert(L % 4 == 0, "L must be a multiple of 4");
+        for (int i = tid; i < rows * (L / 4); i += nthreads) {
+            const int rr = i / (L / 4), j0 = 4 * (i % (L / 4));
             const float4 *xr = xe + rr * XS;
-            float2 acc = make_float2(0.f, 0.f);
-            for (int s = 0; s < Ns; ++s) {
-                const float4 a = xr[s], c = xr[s + j];
-                // a * conj(c)
-                acc.x += a.x * c.x + a.y * c.y;
-                acc.y += a.y * c.x - a.x * c.y;
+            float2 hi[4], lo[4];
+            float4 w0 = xr[j0], w1 = xr[j0 + 1], w2 = xr[j0 + 2];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) hi[q] = lo[q] = make_float2(0.f, 0.f);
+            for (int s0 = 0; s0 < Ns; s0 += 4) {
+                float2 P[4], Q[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) P[q] = Q[q] = make_float2(0.f, 0.f);
+#pragma unroll
+                for (int ss = 0; ss < 4; ++ss) {
+                    const int s = s0 + ss;
+                    if (s < Ns) {
+                        const float4 a = xr[s], w3 = xr[s + j0 + 3];
+                        const float4 c[4] = {w0, w1, w2, w3};
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) {
+                            // a * conj(c): P += (ar, ai).(cr, ci), Q += (ai, -ar).(cr, ci)
+                            P[q] = ffma2(make_float2(a.x, a.y), make_float2(c[q].x, c[q].y), P[q]);
+                            Q[q] = ffma2(make_float2(a.z, a.w), make_float2(c[q].x, c[q].y), Q[q]);
+                        }
+                        w0 = w1;
+                        w1 = w2;
+                        w2 = w3;
+                    }
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q) two_sum_acc(hi[q], lo[q], make_float2(P[q].x + P[q].y, Q[q].x + Q[q].y));
             }
-            cs[i] = acc;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                cs[rr * L + j0 + q] = hi[q];
+                cl[rr * L + j0 + q] = lo[q];
+            }
         }
+        // subarray sums of the centre rows, g[l+1] = g[l] + x[l+Ns] - x[l] (one
+        // thread per row; getCaponC.pyx:246-255 slides them the same way)
         const float invNs = 1.0f / (float)Ns;
-        for (int i = tid; i < TILE * L; i += nthreads) {
-            const int q = i / L, l = i % L;
-            float2 acc = make_float2(0.f, 0.f);
+        for (int q = tid; q < TILE; q += nthreads) {
             if (q + K < rows) {
                 const float4 *xr = xe + (q + K) * XS;
-                for (int s = 0; s < Ns; ++s) {
-                    acc.x += xr[s + l].x;
-                    acc.y += xr[s + l].y;
+                float2 acc = make_float2(0.f, 0.f);
+                for (int s = 0; s < Ns; ++s) acc = fadd2(acc, make_float2(xr[s].x, xr[s].y));
+                for (int l = 0; l < L; ++l) {
+                    gs[q * L + l] = make_float2(acc.x * invNs, acc.y * invNs);
+                    if (l + 1 < L)
+                        acc = fadd2(acc, make_float2(xr[l + Ns].x - xr[l].x, xr[l + Ns].y - xr[l].y));
                 }
             }
-            gs[i] = make_float2(acc.x * invNs, acc.y * invNs);
         }
         __syncthreads();
 
@@ -224,63 +270,100 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
             const float4 *xw = xe + (size_t)lpc * XS;
 
             float2 A[L][NM];
-            // row 0: window sum of c
+            // First covariance row R0[d] = sum_t c_{y+t}[d] (float-float, rounded once),
+            // shared by the group through shared memory.
+            // (the pivot-row buffer is free until the Cholesky; r0 starts G entries in,
+            // so slots below the diagonal, d = j - k > -G, read in-bounds garbage)
+            float2 *r0 = (float2 *)rb + G;
 #pragma unroll
             for (int m = 0; m < NM; ++m) {
                 const int j = m * G + r;
-                float2 acc = make_float2(0.f, 0.f);
-                for (int t = 0; t < T; ++t) acc = fadd2(acc, cs[(lpc + t) * L + j]);
-                A[0][m] = acc;
+                float2 h = make_float2(0.f, 0.f), l = make_float2(0.f, 0.f);
+                for (int t = 0; t < T; ++t) {
+                    two_sum_acc(h, l, cs[(lpc + t) * L + j]);
+                    l = fadd2(l, cl[(lpc + t) * L + j]);
+                }
+                r0[j] = fadd2(h, l);
             }
-            // rows k >= 1: diagonal recurrence, column slot m outer
+            __syncwarp();
+            // Along each diagonal, R[k,k+d] = R0[d] + S[k,k+d] with the increment sums
+            //   S[k,j] = S[k-1,j-1] + D[k,j],
+            //   D[k,j] = sum_t x_t[k-1+Ns] conj(x_t[j-1+Ns]) - x_t[k-1] conj(x_t[j-1]).
+            // D telescopes (S[k,k+d] = sum over the last k subarray rows minus the
+            // first k), so S stays small next to R and its FP32 running sum adds
+            // little rounding; R itself is rounded once, when R0 is added.
+            float2 S[NM];  // current row of S per column slot
+            float tr = 0.f;  // trace over the lane's diagonal entries
+#pragma unroll
+            for (int m = 0; m < NM; ++m) {
+                S[m] = make_float2(0.f, 0.f);
+                A[0][m] = r0[m * G + r];
+            }
+            if (r == 0) tr += A[0][0].x;
+            // column operands (raw complex): x_t[j-1+Ns] and -x_t[j-1], j = m*G + r
+            float2 yn[NM][T], yc[NM][T];
 #pragma unroll
             for (int m = 0; m < NM; ++m) {
                 const int j = m * G + r;
                 const int jm = j > 0 ? j - 1 : 0;
-                // column operands (raw complex): x_t[j-1+Ns] and -x_t[j-1]
-                float2 yn[TMAX], yc[TMAX];
 #pragma unroll
-                for (int t = 0; t < TMAX; ++t) {
-                    if (t < T) {
-                        const float4 a = xw[t * XS + jm + Ns], c = xw[t * XS + jm];
-                        yn[t] = make_float2(a.x, a.y);
-                        yc[t] = make_float2(-c.x, -c.y);
-                    }
-                }
-#pragma unroll
-                for (int k = 1; k < m * G + G; ++k) {
-                    float2 snd;
-                    if (m > 0 && k - 1 < m * G)
-                        snd = (r == G - 1) ? A[k - 1][m - 1] : A[k - 1][m];
-                    else
-                        snd = A[k - 1][m];
-                    const float2 prev = shfl2(snd, (r + G - 1) % G, G);
-                    // x * conj(y) = (xr*yr + xi*yi) + i (xi*yr - xr*yi): with the row
-                    // quad (xr, xi, xi, -xr), accumulate P += (xr,xi).(yr,yi) and
-                    // Q += (xi,-xr).(yr,yi); then re = P.x + P.y, im = Q.x + Q.y.
-                    float2 accP = make_float2(prev.x, 0.f), accQ = make_float2(prev.y, 0.f);
-#pragma unroll
-                    for (int t = 0; t < TMAX; ++t) {
-                        if (t < T) {
-                            const float4 xn = xw[t * XS + k - 1 + Ns];
-                            const float4 xc = xw[t * XS + k - 1];
-                            accP = ffma2(make_float2(xn.x, xn.y), yn[t], accP);
-                            accQ = ffma2(make_float2(xn.z, xn.w), yn[t], accQ);
-                            accP = ffma2(make_float2(xc.x, xc.y), yc[t], accP);
-                            accQ = ffma2(make_float2(xc.z, xc.w), yc[t], accQ);
-                        }
-                    }
-                    A[k][m] = make_float2(accP.x + accP.y, accQ.x + accQ.y);
+                for (int t = 0; t < T; ++t) {
+                    const float4 a = xw[t * XS + jm + Ns], c = xw[t * XS + jm];
+                    yn[m][t] = make_float2(a.x, a.y);
+                    yc[m][t] = make_float2(-c.x, -c.y);
                 }
             }
+            // rows k >= 1, row outer; the previous row of S comes from lane r-1
+            // (lane 0: slot m-1 of lane G-1)
+#pragma unroll
+            for (int k = 1; k < L; ++k) {
+                const int m0 = k / G;  // slots (k, m) exist for m >= k/G
+                float2 prv[NM];
+#pragma unroll
+                for (int m = 0; m < NM; ++m) {
+                    if (m < m0) continue;
+                    float2 sh;
+                    if (m > 0 && k - 1 < m * G)
+                        sh = (r == G - 1) ? S[m - 1] : S[m];
+                    else
+                        sh = S[m];
+                    prv[m] = shfl2(sh, (r + G - 1) % G, G);
+                }
+                // with the row quads (xr, xi, xi, -xr): P += (xr,xi).(yr,yi),
+                // Q += (xi,-xr).(yr,yi), then re = P.x + P.y, im = Q.x + Q.y
+                float2 accP[NM], accQ[NM];
+#pragma unroll
+                for (int m = 0; m < NM; ++m) {
+                    accP[m] = make_float2(0.f, 0.f);
+                    accQ[m] = make_float2(0.f, 0.f);
+                }
+#pragma unroll
+                for (int t = 0; t < T; ++t) {
+                    const float4 xn = xw[t * XS + k - 1 + Ns];
+                    const float4 xc = xw[t * XS + k - 1];
+#pragma unroll
+                    for (int m = 0; m < NM; ++m) {
+                        if (m < m0) continue;
+                        accP[m] = ffma2(make_float2(xn.x, xn.y), yn[m][t], accP[m]);
+                        accQ[m] = ffma2(make_float2(xn.z, xn.w), yn[m][t], accQ[m]);
+                        accP[m] = ffma2(make_float2(xc.x, xc.y), yc[m][t], accP[m]);
+                        accQ[m] = ffma2(make_float2(xc.z, xc.w), yc[m][t], accQ[m]);
+                    }
+                }
+#pragma unroll
+                for (int m = 0; m < NM; ++m) {
+                    if (m < m0) continue;
+                    const float2 dv = make_float2(accP[m].x + accP[m].y, accQ[m].x + accQ[m].y);
+                    S[m] = fadd2(prv[m], dv);
+                    const int d = m * G + r - k;  // diagonal of slot (k, m); < 0 below the diagonal
+                    A[k][m] = fadd2(r0[d], S[m]);
+                    if (k - m * G >= 0 && k - m * G < G && k - m * G == r) tr += A[k][m].x;
+                }
+            }
+            __syncwarp();  // r0 aliases the pivot-row buffer
 
-            // ---- diagonal loading: trace over the lane's diagonal entries
-            float tr = 0.f;
-#pragma unroll
-            for (int m = 0; m < NM; ++m)
-#pragma unroll
-                for (int q = 0; q < G; ++q)
-                    if (q == r) tr += A[m * G + q][m].x;
+            if (C::SYNC) __syncthreads();
+            // ---- diagonal loading d*tr(R)/L
 #pragma unroll
             for (int o = G / 2; o; o >>= 1) tr += __shfl_xor_sync(0xffffffffu, tr, o, G);
             const float dl = f.d * tr / (float)L;
@@ -291,7 +374,7 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
                     if (q == r) A[m * G + q][m].x += dl;
 
             // ---- optional R output (loaded covariance)
-            if (f.R && active) {
+            if (WR && f.R && active) {
                 const size_t pix = (size_t)bx * f.Npy + p;
                 float2 *Rp = f.R + pix * L * L;
                 const float norm = f.r_layout == COS_CAPON_R_REFERENCE ? 1.0f : 1.0f / ((float)Ns * (float)T);
@@ -299,8 +382,8 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
                 for (int m = 0; m < NM; ++m) {
                     const int j = m * G + r;
 #pragma unroll
-                    for (int k = 0; k < m * G + G; ++k) {
-                        if (k <= j) {
+                    for (int k = 0; k < L; ++k) {
+                        if (k < m * G + G && k <= j) {
                             const float2 v = cscale(A[k][m], norm);
                             if (f.r_layout == COS_CAPON_R_REFERENCE) {
                                 Rp[k + (size_t)j * L] = v;
@@ -332,7 +415,8 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
                 const float inv = rsqrtf(dv);
                 // scale row i of the lane's columns; the owner of column i sets U_ii
 #pragma unroll
-                for (int m = mi; m < NM; ++m) A[i][m] = make_float2(A[i][m].x * inv, A[i][m].y * inv);
+                for (int m = 0; m < NM; ++m)
+                    if (m >= mi) A[i][m] = make_float2(A[i][m].x * inv, A[i][m].y * inv);
                 if (r == oi) {
                     A[i][mi] = make_float2(dv * inv, 0.f);
                     b1[mi] = make_float2(b1[mi].x * inv, b1[mi].y * inv);
@@ -340,38 +424,57 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
                 }
                 const float2 y1 = shfl2(b1[mi], oi, G);
                 const float2 y2 = shfl2(b2[mi], oi, G);
-                // publish row i: (-Re, -Re, -Im, +Im) of U[i, j]
-                __syncwarp();
+                // publish row i as (-Re, +Im, -Im, -Re) of U[i, j]: with the consumer's
+                // splats (vr, vr), (vi, vi) of its own U[i, j'] two packed fmas give
+                // A[k][j'] -= conj(U[i,k]) U[i,j']
+                float4 nq[NM];
 #pragma unroll
-                for (int m = mi; m < NM; ++m) {
-                    const float2 v = A[i][m];
-                    rb[m * G + r] = make_float4(-v.x, -v.x, -v.y, v.y);
+                for (int m = 0; m < NM; ++m) {
+                    const float2 v = m >= mi ? A[i][m] : make_float2(0.f, 0.f);
+                    nq[m] = make_float4(-v.x, v.y, -v.y, -v.x);
                 }
                 __syncwarp();
-                // right-hand sides, rows m*G + r > i:  b -= conj(U[i,row]) * y
 #pragma unroll
-                for (int m = mi; m < NM; ++m) {
-                    const float2 u = A[i][m];
-                    const float2 nu1 = make_float2(-u.x, -u.x), nu2 = make_float2(-u.y, u.y);
-                    const bool below = (m * G + r > i);
-                    const float2 t1 = cnmac_conj(b1[m], nu1, nu2, y1);
-                    const float2 t2 = cnmac_conj(b2[m], nu1, nu2, y2);
-                    if (below) {
-                        b1[m] = t1;
-                        b2[m] = t2;
+                for (int m = 0; m < NM; ++m)
+                    if (m >= mi) rb[m * G + r] = nq[m];
+                __syncwarp();
+                // right-hand sides, rows m*G + r > i:  b -= conj(U[i,row]) * y
+                // (for m > mi every row of the slot is below i; for m = mi only r > i%G)
+                {
+                    const float2 y1s = make_float2(y1.y, y1.x), y2s = make_float2(y2.y, y2.x);
+#pragma unroll
+                    for (int m = 0; m < NM; ++m) {
+                        if (m < mi) continue;
+                        const float2 n1 = make_float2(-A[i][m].x, -A[i][m].x), n2 = make_float2(-A[i][m].y, A[i][m].y);
+                        const float2 t1 = ffma2(n2, y1s, ffma2(n1, y1, b1[m]));
+                        const float2 t2 = ffma2(n2, y2s, ffma2(n1, y2, b2[m]));
+                        if (m > mi || r > oi) {
+                            b1[m] = t1;
+                            b2[m] = t2;
+                        }
                     }
                 }
                 // trailing update A[k][j] -= conj(U[i,k]) U[i,j], i < k; slot (k,m) exists for m >= k/G
                 float2 vs[NM];
 #pragma unroll
-                for (int m = mi; m < NM; ++m) vs[m] = A[i][m];
+                for (int m = 0; m < NM; ++m) vs[m] = (m >= mi) ? A[i][m] : make_float2(0.f, 0.f);
+                float2 vrr[NM], vii[NM];
 #pragma unroll
-                for (int k = i + 1; k < L; ++k) {
-                    const float4 u4 = rb[k];
+                for (int m = 0; m < NM; ++m) { vrr[m] = make_float2(vs[m].x, vs[m].x); vii[m] = make_float2(vs[m].y, vs[m].y); }
+                // constant trip counts with compile-time conditions: loops whose
+                // bounds depend on i are otherwise not fully unrolled and the
+                // register matrix would fall back to local memory
 #pragma unroll
-                    for (int m = (k / G > mi ? k / G : mi); m < NM; ++m)
-                        A[k][m] = cnmac_conj(A[k][m], make_float2(u4.x, u4.y), make_float2(u4.z, u4.w), vs[m]);
+                for (int k = 1; k < L; ++k) {
+                    if (k > i) {
+                        const float4 u4 = rb[k];
+#pragma unroll
+                        for (int m = 0; m < NM; ++m)
+                            if (m >= k / G && m >= mi)
+                                A[k][m] = ffma2(vii[m], make_float2(u4.z, u4.w), ffma2(vrr[m], make_float2(u4.x, u4.y), A[k][m]));
+                    }
                 }
+                if (C::SYNC && (i % G) == G - 1) __syncthreads();
             }
 
             // ---- outputs
@@ -395,7 +498,7 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
             }
             if (bad && active && r == 0) atomicOr(status, ERR_NOT_PD);
 
-            if (f.w) {
+            if (WR && f.w) {
                 // back substitution U x = y1, rows L-1 .. 0
                 float2 xv[NM];
 #pragma unroll
@@ -405,8 +508,8 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
                     const int oi = i % G, mi = i / G;
                     float2 part = make_float2(0.f, 0.f);
 #pragma unroll
-                    for (int m = mi; m < NM; ++m)
-                        if (m * G + r > i) part = cadd(part, cmul(A[i][m], xv[m]));
+                    for (int m = 0; m < NM; ++m)
+                        if (m >= mi && m * G + r > i) part = cadd(part, cmul(A[i][m], xv[m]));
 #pragma unroll
                     for (int o = G / 2; o; o >>= 1) part = cadd(part, shfl2_xor(part, o, G));
                     if (r == oi) {
@@ -425,54 +528,42 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
     }
 }
 
-// ---- instantiations and launcher --------------------------------------------
-using Cfg16 = Cfg<16, 4, 4, 2, 5>;
-using Cfg32 = Cfg<32, 8, 4, 2, 5>;
-
-bool fused_supported(int L) { return L == 16 || L == 32; }
-
-template <class C>
-static int launch_cfg(const FramesParam &fp, unsigned *status, int num_sms, cudaStream_t s)
+// ---- launch helper ---------------------------------------------------------
+template <class C, bool WR>
+int launch_cfg(FramesParam fp, unsigned *status, int num_sms, cudaStream_t s)
 {
     const FrameDev &f0 = fp.f[0];
-    if (2 * f0.K + 1 > C::TMAX) return cudaErrorNotSupported;
-    Smem S(C::TILE, f0.K, f0.M, C::L, C::WARPS, C::PPW);
+    if (2 * f0.K + 1 != C::T) return cudaErrorNotSupported;
+    for (int i = 0; i < fp.n; ++i)
+        if (C::M && fp.f[i].M != C::M) return cudaErrorNotSupported;
+    long long begin = 0;
+    for (int i = 0; i < fp.n; ++i) {
+        FrameDev &g = fp.f[i];
+        g.tile = C::TILE;
+        g.tiles_per_beam = (g.Npy + C::TILE - 1) / C::TILE;
+        g.tile_begin = begin;
+        begin += (long long)g.Nx * g.tiles_per_beam;
+    }
+    Smem S(C::TILE, f0.K, C::M ? C::M : f0.M, C::L, C::WARPS, C::PPW);
     if (S.total > 227 * 1024) return cudaErrorNotSupported;
-    cudaError_t e = cudaFuncSetAttribute(fused_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(fused_kernel<C, WR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)S.total);
     if (e != cudaSuccess) return e;
-    const FrameDev &fl = fp.f[fp.n - 1];
-    const long long total = fl.tile_begin + (long long)fl.Nx * fl.tiles_per_beam;
     int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fused_kernel<C>, C::WARPS * 32, S.total);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fused_kernel<C, WR>, C::WARPS * 32, S.total);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorNotSupported;
     long long grid = (long long)num_sms * per_sm;
-    if (grid > total) grid = total;
-    fused_kernel<C><<<(unsigned)grid, C::WARPS * 32, S.total, s>>>(fp, total, status);
+    if (grid > begin) grid = begin;
+    fused_kernel<C, WR><<<(unsigned)grid, C::WARPS * 32, S.total, s>>>(fp, begin, status);
     return cudaGetLastError();
 }
 
-int fused_tile(int L)
+template <class C>
+int launch_any(const FramesParam &fp, bool wr, unsigned *status, int num_sms, cudaStream_t s)
 {
-    if (L == 16) return Cfg16::TILE;
-    if (L == 32) return Cfg32::TILE;
-    return 0;
+    return wr ? launch_cfg<C, true>(fp, status, num_sms, s) : launch_cfg<C, false>(fp, status, num_sms, s);
 }
 
-int fused_tmax(int L)
-{
-    if (L == 16) return Cfg16::TMAX;
-    if (L == 32) return Cfg32::TMAX;
-    return 0;
-}
-
-int launch_fused_frames(const FramesParam &fp, unsigned *status, int num_sms, cudaStream_t s)
-{
-    const int L = fp.f[0].L;
-    if (L == 16) return launch_cfg<Cfg16>(fp, status, num_sms, s);
-    if (L == 32) return launch_cfg<Cfg32>(fp, status, num_sms, s);
-    return cudaErrorNotSupported;
-}
-
+}  // namespace fused
 }  // namespace cgb

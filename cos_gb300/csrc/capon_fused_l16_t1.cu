@@ -1,0 +1,34 @@
+// Fused element-space kernel instantiations for L = 16, temporal window T = 1.
+// The autotuner in capon_api.cu picks one per (L, K, M) shape; a candidate
+// compiled for a fixed M reports cudaErrorNotSupported for other M.
+#include "capon_fused.cuh"
+
+namespace cgb {
+namespace {
+int launch_0(const FramesParam &fp, bool wr, unsigned *st, int n, cudaStream_t s)
+{
+    return fused::launch_any<fused::Cfg<16, 4, 8, 1, 1, 32, true>>(fp, wr, st, n, s);
+}
+int launch_1(const FramesParam &fp, bool wr, unsigned *st, int n, cudaStream_t s)
+{
+    return fused::launch_any<fused::Cfg<16, 8, 8, 1, 1, 32, true>>(fp, wr, st, n, s);
+}
+int launch_2(const FramesParam &fp, bool wr, unsigned *st, int n, cudaStream_t s)
+{
+    return fused::launch_any<fused::Cfg<16, 4, 8, 1, 1, 0, true>>(fp, wr, st, n, s);
+}
+
+const FusedCandidate kCand[] = {
+    {"L16.G4.W8.N1.sync.M32.T1", 16, 1, 32, launch_0},
+    {"L16.G8.W8.N1.sync.M32.T1", 16, 1, 32, launch_1},
+    {"L16.G4.W8.N1.sync.T1", 16, 1, 0, launch_2},
+};
+}  // namespace
+
+int fused_candidates_l16_t1(const FusedCandidate **out)
+{
+    *out = kCand;
+    return (int)(sizeof(kCand) / sizeof(kCand[0]));
+}
+
+}  // namespace cgb

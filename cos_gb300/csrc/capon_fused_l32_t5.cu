@@ -1,0 +1,34 @@
+// Fused element-space kernel instantiations for L = 32, temporal window T = 5.
+// The autotuner in capon_api.cu picks one per (L, K, M) shape; a candidate
+// compiled for a fixed M reports cudaErrorNotSupported for other M.
+#include "capon_fused.cuh"
+
+namespace cgb {
+namespace {
+int launch_0(const FramesParam &fp, bool wr, unsigned *st, int n, cudaStream_t s)
+{
+    return fused::launch_any<fused::Cfg<32, 8, 8, 2, 5, 64, true>>(fp, wr, st, n, s);
+}
+int launch_1(const FramesParam &fp, bool wr, unsigned *st, int n, cudaStream_t s)
+{
+    return fused::launch_any<fused::Cfg<32, 16, 8, 2, 5, 64, true>>(fp, wr, st, n, s);
+}
+int launch_2(const FramesParam &fp, bool wr, unsigned *st, int n, cudaStream_t s)
+{
+    return fused::launch_any<fused::Cfg<32, 8, 8, 2, 5, 0, true>>(fp, wr, st, n, s);
+}
+
+const FusedCandidate kCand[] = {
+    {"L32.G8.W8.N2.sync.M64.T5", 32, 5, 64, launch_0},
+    {"L32.G16.W8.N2.sync.M64.T5", 32, 5, 64, launch_1},
+    {"L32.G8.W8.N2.sync.T5", 32, 5, 0, launch_2},
+};
+}  // namespace
+
+int fused_candidates_l32_t5(const FusedCandidate **out)
+{
+    *out = kCand;
+    return (int)(sizeof(kCand) / sizeof(kCand[0]));
+}
+
+}  // namespace cgb

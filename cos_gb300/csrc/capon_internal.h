@@ -46,13 +46,22 @@ int launch_plain_solve_hpd(const FrameDev &f, const float2 *R, float2 *Ria, unsi
 int launch_plain_output(const FrameDev &f, const float2 *Ria, cudaStream_t s);
 // general batched LU solve, column-major A
 int launch_lu_solve(float2 *x, const float2 *A, const float2 *b, int N, int batch, cudaStream_t s);
-// fused element-space path; returns cudaErrorNotSupported when L has no instantiation.
-// fp.f[i].tile_begin / tiles_per_beam must use fused_tile(L)-sized tiles; all
+// fused element-space path: candidate configurations per subarray length.
+// A candidate's launch fills the tiling fields of the frames itself; all
 // frames of one launch share L, K and M.
-bool fused_supported(int L);
-int fused_tile(int L);
-int fused_tmax(int L);  // largest 2K+1 the instantiation holds
-int launch_fused_frames(const FramesParam &fp, unsigned *status, int num_sms, cudaStream_t s);
+struct FusedCandidate {
+    const char *name;
+    int L;
+    int T;  // the temporal window 2K+1 the instantiation is compiled for
+    int M;  // the channel count it is compiled for, 0 = any
+    int (*launch)(const FramesParam &fp, bool want_w_or_R, unsigned *status, int num_sms, cudaStream_t s);
+};
+int fused_candidates_l16_t1(const FusedCandidate **out);
+int fused_candidates_l16_t3(const FusedCandidate **out);
+int fused_candidates_l16_t5(const FusedCandidate **out);
+int fused_candidates_l32_t1(const FusedCandidate **out);
+int fused_candidates_l32_t3(const FusedCandidate **out);
+int fused_candidates_l32_t5(const FusedCandidate **out);
 // beamspace path (Nb > 0)
 int launch_beamspace(const FrameDev &f, float2 *R_out, cudaStream_t s);
 int launch_butler(float2 *B, int Nb, int L, cudaStream_t s);
