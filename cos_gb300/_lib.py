@@ -26,7 +26,7 @@ R_REFERENCE, R_NORMALISED = 0, 1
 EXPORTS = (
     "cos_capon_create", "cos_capon_destroy", "cos_capon_get_capon", "cos_capon_get_capon_ex",
     "cos_capon_run", "cos_capon_build_r", "cos_capon_solve", "cos_capon_butler",
-    "cos_capon_device_status", "cos_capon_status_string",
+    "cos_capon_device_status", "cos_capon_status_string", "cos_capon_run_plain_noalloc",
 )
 
 
@@ -65,6 +65,7 @@ def _load() -> C.CDLL:
         "cos_capon_butler": [vp, vp, i, i, i],
         "cos_capon_device_status": [vp],
         "cos_capon_status_string": [i],
+        "cos_capon_run_plain_noalloc": [C.POINTER(Frame), vp],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)

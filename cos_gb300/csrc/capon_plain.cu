@@ -9,6 +9,8 @@
 //   * the general path for subarray lengths the fused kernel does not
 //     instantiate.
 // The general LU solver for cos_capon_solve (ISolver::solve) is here too.
+#include <string.h>
+
 #include "capon_common.cuh"
 #include "capon_internal.h"
 #include "../../include/cos_capon.h"
@@ -295,4 +297,85 @@ int launch_lu_solve(float2 *x, const float2 *A, const float2 *b, int N, int batc
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free entry point (no counterpart in the reference).
+//
+// Some callers cannot call cudaMalloc: code that runs inside another
+// framework's memory pool or allocator callback, real-time loops that must
+// not reach the driver's allocator, or processes whose device memory is
+// reserved up front.  cos_capon_run_plain_noalloc runs the plain three-stage
+// pipeline with its two work buffers (per-pixel covariance and R^-1 a) and its
+// status word taken from file-scope __device__ arrays of fixed size, so it
+// allocates nothing.  Every GPU that loads this library holds these arrays
+// (about 8 MiB) until the process exits.
+// ---------------------------------------------------------------------------
+#define COS_NOALLOC_SCRATCH_ELEMS (1u << 20)  // float2 elements: 8 MiB
+
+static __device__ __align__(256) float2 g_noalloc_scratch[COS_NOALLOC_SCRATCH_ELEMS];
+static __device__ __align__(256) unsigned g_noalloc_status[64];
+
+namespace {
+constexpr int kMaxDevices = 64;
+float2 *g_scratch_ptr[kMaxDevices];
+unsigned *g_status_ptr[kMaxDevices];
+
+// Device addresses of the static arrays for the current device, looked up once
+// per device (the names are host-side stand-ins, not device addresses).
+int noalloc_setup(float2 **scratch, unsigned **status)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    if (!g_scratch_ptr[dev]) {
+        void *ps = nullptr, *pt = nullptr;
+        if ((e = cudaGetSymbolAddress(&ps, g_noalloc_scratch)) != cudaSuccess) return e;
+        if ((e = cudaGetSymbolAddress(&pt, g_noalloc_status)) != cudaSuccess) return e;
+        g_status_ptr[dev] = (unsigned *)pt;
+        g_scratch_ptr[dev] = (float2 *)ps;
+    }
+    *scratch = g_scratch_ptr[dev];
+    *status = g_status_ptr[dev];
+    return cudaSuccess;
+}
+}  // namespace
+
 }  // namespace cgb
+
+extern "C" int cos_capon_run_plain_noalloc(const cos_capon_frame *fr, void *stream)
+{
+    using namespace cgb;
+    if (!fr || !fr->x || !fr->z) return COS_CAPON_ERR_INVALID_VALUE;
+    const int L = fr->L, K = fr->K, M = fr->M, Nx = fr->Nx, Ny = fr->Ny;
+    if (Nx < 1 || Ny < 1 || L < 1 || M < 1 || K < 0 || fr->Nb != 0 || L > M || 2 * K >= Ny)
+        return COS_CAPON_ERR_LAUNCH;
+    if (L > 64) return COS_CAPON_ERR_NOT_SUPPORTED;
+    const size_t npix = (size_t)Nx * (Ny - 2 * K);
+    const size_t need = npix * ((size_t)L * L + (size_t)L);
+    if (need > COS_NOALLOC_SCRATCH_ELEMS) return COS_CAPON_ERR_OUT_OF_MEMORY;
+    float2 *scratch = nullptr;
+    unsigned *status = nullptr;
+    int e = noalloc_setup(&scratch, &status);
+    if (e) return e;
+    cudaStream_t s = (cudaStream_t)stream;
+    FrameDev f;
+    memset(&f, 0, sizeof(f));
+    f.x = (const float2 *)fr->x;
+    f.z = (float2 *)fr->z;
+    f.P = fr->P;
+    f.w = (float2 *)fr->w;
+    f.d = fr->d;
+    f.L = L;
+    f.K = K;
+    f.M = M;
+    f.Nx = Nx;
+    f.Ny = Ny;
+    f.Npy = Ny - 2 * K;
+    float2 *Rw = scratch, *Ria = scratch + npix * (size_t)L * L;
+    // the status word keeps the previous call's value: clear it first
+    if ((e = cudaMemsetAsync(status, 0, sizeof(unsigned), s)) != cudaSuccess) return e;
+    if ((e = launch_plain_build_r(f, Rw, 1, s))) return e;
+    if ((e = launch_plain_solve_hpd(f, Rw, Ria, status, s))) return e;
+    if ((e = launch_plain_output(f, Ria, s))) return e;
+    return 0;
+}

@@ -126,6 +126,20 @@ int cos_capon_butler(cos_capon_ctx *ctx, void *B, int Nb, int L, int B_on_gpu);
  * when a bounded device-side wait gave up).  Synchronises the context stream. */
 int cos_capon_device_status(cos_capon_ctx *ctx);
 
+/* No counterpart in the reference.  Allocation-free variant of the plain FP32
+ * three-stage pipeline for callers that cannot allocate device memory (code
+ * running inside another framework's allocator, real-time loops that must not
+ * call into the driver's allocator).  Its work buffers are a fixed file-scope
+ * device array of 2^20 complex elements (8 MiB, held by every GPU that loads
+ * the library until exit): frames with Nx*(Ny-2K)*(L*L+L) above that return
+ * COS_CAPON_ERR_OUT_OF_MEMORY.  Element space only (Nb = 0), device pointers,
+ * asynchronous on `stream` (a cudaStream_t, NULL = default stream); no
+ * context, no cudaMalloc/cudaFree.  The first call on a device looks up the
+ * array's device address; make that first call before any stream capture.
+ * All calls share the array, so calls that overlap on the GPU (different
+ * streams, or threads) race and must be serialised by the caller. */
+int cos_capon_run_plain_noalloc(const cos_capon_frame *frame, void *stream);
+
 /* Human-readable text for a status code. */
 const char *cos_capon_status_string(int status);
 
