@@ -53,8 +53,8 @@ struct cos_capon_ctx {
     unsigned *d_status = nullptr;
     // host-pointer call buffers
     DevBuf x, z, P, w, R;
-    // plain-pipeline scratch
-    DevBuf Rwork, Ria;
+    // plain / precise pipeline scratch
+    DevBuf Rwork, Rlo, dl, Ria;
     // stage entry points
     DevBuf A, b, sol;
     // autotuner: chosen fused candidate per (L, K, M, w-or-R requested)
@@ -126,7 +126,7 @@ static int candidates(int L, int K, const FusedCandidate **out)
 
 static bool use_fused(const FrameDev &f, const cos_capon_opts &o)
 {
-    if (o.form != COS_CAPON_FORM_FUSED || f.Nb != 0) return false;
+    if (o.form != COS_CAPON_FORM_FUSED || f.Nb != 0 || o.refine) return false;
     const FusedCandidate *c = nullptr;
     const int n = candidates(f.L, f.K, &c);
     for (int i = 0; i < n; ++i)
@@ -221,6 +221,23 @@ static int run_plain(cos_capon_ctx *c, FrameDev f, cudaStream_t s)
     return e;
 }
 
+// precise pipeline (float-float covariance, FP32 Cholesky, optional FP64-residual
+// refinement) for one element-space frame
+static int run_precise(cos_capon_ctx *c, FrameDev f, bool refine, cudaStream_t s)
+{
+    const size_t npix = (size_t)f.Nx * f.Npy;
+    int e;
+    if ((e = c->Rwork.ensure(npix * f.L * f.L * sizeof(float2)))) return e;
+    if ((e = c->Rlo.ensure(npix * f.L * f.L * sizeof(float2)))) return e;
+    if ((e = c->dl.ensure(npix * sizeof(float)))) return e;
+    if ((e = c->Ria.ensure(npix * f.L * sizeof(float2)))) return e;
+    if ((e = launch_precise(f, (float2 *)c->Rwork.p, (float2 *)c->Rlo.p, (float *)c->dl.p, (float2 *)c->Ria.p,
+                            c->d_status, refine, s)))
+        return e;
+    if (f.R) e = launch_plain_build_r(f, f.R, f.r_layout == COS_CAPON_R_REFERENCE ? 1 : 0, s);
+    return e;
+}
+
 static int run_frames(cos_capon_ctx *c, const FrameDev *fs, int n, const cos_capon_opts &o, cudaStream_t s)
 {
     // batch consecutive fused frames with equal (L, K, M) into one launch
@@ -251,7 +268,10 @@ static int run_frames(cos_capon_ctx *c, const FrameDev *fs, int n, const cos_cap
             }
             ++i;
         } else {
-            int e = run_plain(c, f, s);
+            // element space without a fused instantiation (or with refinement):
+            // the precise pipeline; the plain form when asked for
+            int e = (o.form == COS_CAPON_FORM_PLAIN && !o.refine) ? run_plain(c, f, s)
+                                                                  : run_precise(c, f, o.refine != 0, s);
             if (e) return e;
             ++i;
         }
@@ -303,7 +323,9 @@ int cos_capon_destroy(cos_capon_ctx *c)
 {
     if (!c) return COS_CAPON_ERR_INVALID_VALUE;
     cudaStreamSynchronize(c->stream);
-    for (DevBuf *b : {&c->x, &c->z, &c->P, &c->w, &c->R, &c->Rwork, &c->Ria, &c->A, &c->b, &c->sol}) b->release();
+    for (DevBuf *b : {&c->x, &c->z, &c->P, &c->w, &c->R, &c->Rwork, &c->Rlo, &c->dl, &c->Ria, &c->A, &c->b,
+                      &c->sol})
+        b->release();
     if (c->d_status) cudaFree(c->d_status);
     if (c->stream) cudaStreamDestroy(c->stream);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -317,7 +339,6 @@ int cos_capon_run(cos_capon_ctx *c, const cos_capon_frame *frames, int nframes, 
 {
     if (!c || !frames || nframes < 1) return COS_CAPON_ERR_INVALID_VALUE;
     const cos_capon_opts o = opts ? *opts : kDefaultOpts;
-    if (o.refine) return COS_CAPON_ERR_NOT_SUPPORTED;
     std::vector<FrameDev> fs;
     fs.reserve(nframes);
     for (int i = 0; i < nframes; ++i) {
@@ -339,7 +360,6 @@ int cos_capon_get_capon_ex(cos_capon_ctx *c, void *z, float *P, void *w, void *R
     if (e) return e;
     if (!x || !z) return COS_CAPON_ERR_INVALID_VALUE;
     const cos_capon_opts o = opts ? *opts : kDefaultOpts;
-    if (o.refine) return COS_CAPON_ERR_NOT_SUPPORTED;
     const size_t N = (size_t)Nx * Nz, npix = (size_t)Nx * (Nz - 2 * Yavg);
     const size_t bx = N * M * sizeof(float2), bz = npix * sizeof(float2), bp = npix * sizeof(float),
                  bw = npix * L * sizeof(float2), bR = npix * L * L * sizeof(float2);
@@ -356,7 +376,10 @@ int cos_capon_get_capon_ex(cos_capon_ctx *c, void *z, float *P, void *w, void *R
     need += (P && bp > c->P.cap) ? bp : 0;
     need += (w && bw > c->w.cap) ? bw : 0;
     need += (R && bR > c->R.cap) ? bR : 0;
-    if (plain && Nb == 0) need += (bR > c->Rwork.cap ? bR : 0) + (bw > c->Ria.cap ? bw : 0);
+    if (plain && Nb == 0) {
+        need += (bR > c->Rwork.cap ? bR : 0) + (bw > c->Ria.cap ? bw : 0);
+        if (!(o.form == COS_CAPON_FORM_PLAIN && !o.refine)) need += bR > c->Rlo.cap ? bR : 0;
+    }
     if ((e = check_free(need))) return e;
     if ((e = c->x.ensure(bx)) || (e = c->z.ensure(bz))) return e;
     if (P && (e = c->P.ensure(bp))) return e;

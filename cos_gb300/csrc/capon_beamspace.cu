@@ -30,7 +30,7 @@ struct BsSmem {
     {
         const int T = 2 * K + 1, Ns = M - L + 1;
         ld = Nb + 1;
-        per_warp = (size_t)T * M + (size_t)T * Ns * Nb + (size_t)Nb * ld + 2 * (size_t)Nb + 2;
+        per_warp = (size_t)T * M + (size_t)T * Ns * Nb + 3 * (size_t)Nb * ld + 2 * (size_t)Nb + 2;
         table = (size_t)Nb * L + 2 * (size_t)Nb;
         total = (table + kBsWarps * per_warp) * sizeof(float2);
     }
@@ -50,7 +50,9 @@ beamspace_kernel(FrameDev f, float2 *__restrict__ Rbs)
     float2 *xs = ws;                              // T x M
     float2 *Y = xs + (size_t)T * M;               // T x Ns x Nb
     float2 *Cm = Y + (size_t)T * Ns * Nb;         // Nb x ld
-    float2 *xb = Cm + (size_t)Nb * S.ld;          // Nb
+    float2 *Ch = Cm + (size_t)Nb * S.ld;          // Nb x ld: R_bs high part (float-float)
+    float2 *Cl = Ch + (size_t)Nb * S.ld;          // Nb x ld: R_bs low part
+    float2 *xb = Cl + (size_t)Nb * S.ld;          // Nb
     const float isl = 1.0f / sqrtf((float)L);
 
     for (int i = threadIdx.x; i < Nb * L; i += blockDim.x) {
@@ -125,12 +127,17 @@ beamspace_kernel(FrameDev f, float2 *__restrict__ Rbs)
             two_sum_acc(hi, lo, acc);
         }
         const float2 v = fadd2(hi, lo);
+        const float2 vl = fsub2(lo, fsub2(v, hi));  // v + vl == hi + lo
         Cm[bb * S.ld + cc] = v;
         Cm[cc * S.ld + bb] = cconj(v);
+        Ch[bb * S.ld + cc] = v;
+        Ch[cc * S.ld + bb] = cconj(v);
+        Cl[bb * S.ld + cc] = vl;
+        Cl[cc * S.ld + bb] = cconj(vl);
     }
     __syncwarp();
+    float dl = 0.f;
     if (lane == 0) {
-        float dl;
         if (f.loading == COS_CAPON_LOAD_BEAMSPACE) {
             float tb = 0.f;
             for (int i = 0; i < Nb; ++i) tb += Cm[i * S.ld + i].x;
@@ -146,7 +153,12 @@ beamspace_kernel(FrameDev f, float2 *__restrict__ Rbs)
         for (int i = lane; i < Nb * Nb; i += 32) Rp[i] = Cm[(i % Nb) * S.ld + i / Nb];
     }
     __syncwarp();
-    // Cholesky (upper, row-major in Cm) and the two triangular solves for a_bs
+    // FP32 Cholesky (upper, row-major in Cm) and the two triangular solves for
+    // a_bs, then one step of iterative refinement: the residual
+    // r = a_bs - (R_hi + R_lo + dl I) x0 is formed in FP64 from the float-float
+    // matrix -- the Butler transform gathers a scatterer into one beam, so a
+    // single FP32 rounding of R_bs already perturbs the small eigenvalues by
+    // ~1e-4 -- and the correction is solved with the same FP32 factor.
     if (lane == 0) {
         for (int i = 0; i < Nb; ++i) {
             float dv = Cm[i * S.ld + i].x;
@@ -159,15 +171,35 @@ beamspace_kernel(FrameDev f, float2 *__restrict__ Rbs)
                 Cm[i * S.ld + j] = cscale(v, iu);
             }
         }
-        for (int i = 0; i < Nb; ++i) {
-            float2 v = ab[i];
-            for (int k = 0; k < i; ++k) v = csub(v, cconjmul(Cm[k * S.ld + i], xb[k]));
-            xb[i] = cscale(v, 1.0f / Cm[i * S.ld + i].x);
-        }
-        for (int i = Nb - 1; i >= 0; --i) {
-            float2 v = xb[i];
-            for (int k = i + 1; k < Nb; ++k) v = csub(v, cmul(Cm[i * S.ld + k], xb[k]));
-            xb[i] = cscale(v, 1.0f / Cm[i * S.ld + i].x);
+        for (int pass = 0; pass < 2; ++pass) {
+            // right-hand side: a_bs (pass 0) or the FP64 residual (pass 1); the
+            // solution is built in Cm's padding column (index Nb)
+            for (int i = 0; i < Nb; ++i) {
+                float2 v;
+                if (pass == 0) {
+                    v = ab[i];
+                } else {
+                    double rr = (double)ab[i].x, ri = (double)ab[i].y;
+                    for (int j = 0; j < Nb; ++j) {
+                        const double ar = (double)Ch[i * S.ld + j].x + (double)Cl[i * S.ld + j].x +
+                                          (i == j ? (double)dl : 0.0);
+                        const double ai = (double)Ch[i * S.ld + j].y + (double)Cl[i * S.ld + j].y;
+                        const double xr = (double)xb[j].x, xi = (double)xb[j].y;
+                        rr -= ar * xr - ai * xi;
+                        ri -= ar * xi + ai * xr;
+                    }
+                    v = make_float2((float)rr, (float)ri);
+                }
+                // forward U^H y = v
+                for (int k = 0; k < i; ++k) v = csub(v, cconjmul(Cm[k * S.ld + i], Cm[k * S.ld + Nb]));
+                Cm[i * S.ld + Nb] = cscale(v, 1.0f / Cm[i * S.ld + i].x);
+            }
+            for (int i = Nb - 1; i >= 0; --i) {
+                float2 v = Cm[i * S.ld + Nb];
+                for (int k = i + 1; k < Nb; ++k) v = csub(v, cmul(Cm[i * S.ld + k], Cm[k * S.ld + Nb]));
+                Cm[i * S.ld + Nb] = cscale(v, 1.0f / Cm[i * S.ld + i].x);
+            }
+            for (int i = 0; i < Nb; ++i) xb[i] = pass == 0 ? Cm[i * S.ld + Nb] : cadd(xb[i], Cm[i * S.ld + Nb]);
         }
     }
     __syncwarp();

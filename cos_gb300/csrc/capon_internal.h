@@ -44,6 +44,10 @@ int launch_plain_build_r(const FrameDev &f, float2 *R_out, int r_ref_layout, cud
 int launch_plain_solve_hpd(const FrameDev &f, const float2 *R, float2 *Ria, unsigned *status,
                            cudaStream_t s);
 int launch_plain_output(const FrameDev &f, const float2 *Ria, cudaStream_t s);
+// precise element-space pipeline (float-float covariance, FP32 Cholesky,
+// optional FP64-residual refinement); Rhi/Rlo hold Nx*Npy*L*L, dl Nx*Npy, Ria Nx*Npy*L
+int launch_precise(const FrameDev &f, float2 *Rhi, float2 *Rlo, float *dl, float2 *Ria, unsigned *status,
+                   bool refine, cudaStream_t s);
 // general batched LU solve, column-major A
 int launch_lu_solve(float2 *x, const float2 *A, const float2 *b, int N, int batch, cudaStream_t s);
 // fused element-space path: candidate configurations per subarray length.

@@ -234,3 +234,42 @@ def test_full_size_config1_properties(cap):
     sub = np.ascontiguousarray(x[beams])
     ref = oracle.capon(sub, c["d"], c["L"], c["K"], want_w=False, nthreads=3)
     assert_close(z1[beams], P1[beams], None, ref, what="config1 full-size sampled beams")
+
+
+@pytest.mark.parametrize("L,K,d,M", [(64, 4, 1e-3, 128), (48, 1, 0.01, 96)])
+def test_precise_pipeline_and_refinement(cap, L, K, d, M):
+    """Subarray lengths without a fused instantiation run the precise pipeline
+    (float-float covariance, FP32 Cholesky); refine=1 adds one correction step
+    with an FP64 residual.  Config-3 stress case (two coherent scatterers one
+    beam apart at 40 dB, loading 1e-3) for L=64."""
+    from cos_gb300 import _lib, synth
+    if L == 64:
+        x = synth.cube(96, 3, M, [100.0, 100.0], seed=3, coherent_pair=True)
+    else:
+        x = synth.cube(96, 3, M, [10.0, 5.0], seed=7)
+    ref = oracle.capon(x, d, L, K, nthreads=3)
+    z, P, w = cap.getCaponGPU(x, d, L, K)
+    assert_close(z, P, w, ref, what=f"precise L{L}")
+    zr, Pr, wr = cap.Capon(), None, None
+    Npy = x.shape[1] - 2 * K
+    zr = np.zeros((3, Npy), np.complex64)
+    Pr = np.zeros((3, Npy), np.float32)
+    wr = np.zeros((3, Npy, L), np.complex64)
+    rc = cap.Capon().getCaponEx(zr, Pr, wr, None, x, d, L, K, M, 3, x.shape[1], 0, cap.opts(refine=1))
+    assert rc == 0
+    e = errors(zr, Pr, wr, ref)
+    print(f"refined L{L}: P max {e['P'].max():.2e}, w max {e['w'].max():.2e}")
+    assert e["P"].max() <= 1e-6 and e["w"].max() <= 1e-4
+
+
+def test_refinement_option_on_fused_shape(cap):
+    from cos_gb300 import synth
+    c = synth.config1(seed=1, Nx=3, Ny=256)
+    x = c["x"]
+    Npy = x.shape[1] - 2 * c["K"]
+    z = np.zeros((3, Npy), np.complex64)
+    P = np.zeros((3, Npy), np.float32)
+    assert cap.Capon().getCaponEx(z, P, None, None, x, c["d"], c["L"], c["K"], 64, 3, x.shape[1], 0,
+                                  cap.opts(refine=1)) == 0
+    ref = oracle.capon(x, c["d"], c["L"], c["K"], want_w=False, nthreads=3)
+    assert np.max(np.abs(P - ref["P"]) / ref["P"]) <= 1e-6
