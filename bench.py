@@ -281,6 +281,36 @@ def run_gpu(args) -> None:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_ms = float(t.item())
 
+    # adjoint cost: forward with the weights saved (absolute loading, as the
+    # differentiable path runs it) and the adjoint kernel over the full frame
+    adj = None
+    try:
+        from cos_gb300.autograd import capon_power
+        delta = torch.tensor(0.5, dtype=torch.float32, device="cuda", requires_grad=True)
+        tau = torch.zeros(M, dtype=torch.float32, device="cuda", requires_grad=True)
+        xg = xt.clone().requires_grad_(True)
+        for _ in range(2):
+            Pd = capon_power(xg, delta, tau, L, K, 0.25, ctx)
+            Pd.sum().backward()
+        torch.cuda.synchronize()
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        nrep = max(2, min(args.steps, 5))
+        fw = bw = 0.0
+        for _ in range(nrep):
+            e0.record()
+            Pd = capon_power(xg, delta, tau, L, K, 0.25, ctx)
+            e1.record()
+            Pd.sum().backward()
+            e2.record()
+            e2.synchronize()
+            fw += e0.elapsed_time(e1)
+            bw += e1.elapsed_time(e2)
+        adj = {"forward_ms": fw / nrep, "backward_ms": bw / nrep, "backward_over_forward": bw / fw,
+               "note": "full frame, loss = sum of P; forward saves w (the ms include the torch glue: phase, "
+                       "gradient buffers)"}
+    except Exception as exc:  # reported, not fatal to the throughput line
+        adj = {"error": str(exc)[:200]}
+
     # parity of this very run against the FP64 oracle on sampled beams
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle  # noqa: E402
@@ -318,6 +348,7 @@ def run_gpu(args) -> None:
                          "frac": (achieved_gbs / hbm_peak) if hbm_peak else None,
                          "bytes_per_pixel": BYTES_PER_PIXEL, "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
         "clocks": clocks,
+        "adjoint": adj,
     }
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = {k: v for k, v in cpu_reference_rate(os.cpu_count() or 1, 16).items()

@@ -19,7 +19,7 @@ ERR_NOT_SUPPORTED = 801
 ERR_TIMEOUT = 909
 
 FORM_FUSED, FORM_PLAIN = 0, 1
-LOAD_ELEMENT, LOAD_BEAMSPACE = 0, 1
+LOAD_ELEMENT, LOAD_BEAMSPACE, LOAD_ABSOLUTE = 0, 1, 2
 R_REFERENCE, R_NORMALISED = 0, 1
 
 # every symbol include/cos_capon.h declares
@@ -27,6 +27,7 @@ EXPORTS = (
     "cos_capon_create", "cos_capon_destroy", "cos_capon_get_capon", "cos_capon_get_capon_ex",
     "cos_capon_run", "cos_capon_build_r", "cos_capon_solve", "cos_capon_butler",
     "cos_capon_device_status", "cos_capon_status_string", "cos_capon_run_plain_noalloc",
+    "cos_capon_backward",
 )
 
 
@@ -40,6 +41,12 @@ class Frame(C.Structure):
         ("d", C.c_float), ("L", C.c_int), ("K", C.c_int), ("M", C.c_int), ("Nx", C.c_int),
         ("Ny", C.c_int), ("Nb", C.c_int),
     ]
+
+
+class Adjoint(C.Structure):
+    _fields_ = [("x", C.c_void_p), ("w", C.c_void_p), ("gP", C.c_void_p), ("gx", C.c_void_p),
+                ("gd", C.c_void_p), ("gtheta", C.c_void_p), ("L", C.c_int), ("K", C.c_int), ("M", C.c_int),
+                ("Nx", C.c_int), ("Ny", C.c_int)]
 
 
 class CaponError(RuntimeError):
@@ -66,6 +73,7 @@ def _load() -> C.CDLL:
         "cos_capon_device_status": [vp],
         "cos_capon_status_string": [i],
         "cos_capon_run_plain_noalloc": [C.POINTER(Frame), vp],
+        "cos_capon_backward": [vp, C.POINTER(Adjoint), vp],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)

@@ -173,7 +173,8 @@ class DeviceFrame:
 def capon_frames(frames: Sequence[DeviceFrame], ctx: Optional[Context] = None, o: Optional[Opts] = None,
                  stream=None) -> None:
     """Run all frames in one call on `stream` (torch stream or raw handle;
-    default: the current torch stream).  Asynchronous."""
+    default: the current torch stream, whose handle is 0 for the default
+    stream).  Asynchronous."""
     import torch
     ctx = ctx or _module_ctx()
     for f in frames:

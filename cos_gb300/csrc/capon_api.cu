@@ -348,7 +348,9 @@ int cos_capon_run(cos_capon_ctx *c, const cos_capon_frame *frames, int nframes, 
         if (!fr.x || !fr.z) return COS_CAPON_ERR_INVALID_VALUE;
         fs.push_back(make_frame(fr, o));
     }
-    cudaStream_t s = stream ? (cudaStream_t)stream : c->stream;
+    // NULL is the default stream, as everywhere in CUDA; the context's own
+    // stream serves only the host-pointer calls
+    cudaStream_t s = (cudaStream_t)stream;
     return run_frames(c, fs.data(), nframes, o, s);
 }
 
@@ -509,6 +511,27 @@ int cos_capon_butler(cos_capon_ctx *c, void *B, int Nb, int L, int B_on_gpu)
     cudaError_t ce;
     if (!B_on_gpu && (ce = cudaMemcpyAsync(B, Bd, bytes, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return ce;
     return read_status(c, s, true);
+}
+
+int cos_capon_backward(cos_capon_ctx *c, const cos_capon_adjoint *adj, void *stream)
+{
+    if (!c || !adj || !adj->x || !adj->w || !adj->gP || !adj->gx) return COS_CAPON_ERR_INVALID_VALUE;
+    int e = check_sizes(adj->L, adj->K, adj->M, adj->Nx, adj->Ny, 0);
+    if (e) return e;
+    AdjDev a;
+    a.x = (const float2 *)adj->x;
+    a.w = (const float2 *)adj->w;
+    a.gP = adj->gP;
+    a.gx = (float2 *)adj->gx;
+    a.gd = adj->gd;
+    a.gth = adj->gtheta;
+    a.L = adj->L;
+    a.K = adj->K;
+    a.M = adj->M;
+    a.Nx = adj->Nx;
+    a.Ny = adj->Ny;
+    a.Npy = adj->Ny - 2 * adj->K;
+    return launch_adjoint(a, c->num_sms, (cudaStream_t)stream);
 }
 
 int cos_capon_device_status(cos_capon_ctx *c)

@@ -138,7 +138,9 @@ beamspace_kernel(FrameDev f, float2 *__restrict__ Rbs)
     __syncwarp();
     float dl = 0.f;
     if (lane == 0) {
-        if (f.loading == COS_CAPON_LOAD_BEAMSPACE) {
+        if (f.loading == COS_CAPON_LOAD_ABSOLUTE) {
+            dl = f.d * (float)(Ns * T);
+        } else if (f.loading == COS_CAPON_LOAD_BEAMSPACE) {
             float tb = 0.f;
             for (int i = 0; i < Nb; ++i) tb += Cm[i * S.ld + i].x;
             dl = f.d * tb / (float)Nb;

@@ -366,7 +366,8 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
             // ---- diagonal loading d*tr(R)/L
 #pragma unroll
             for (int o = G / 2; o; o >>= 1) tr += __shfl_xor_sync(0xffffffffu, tr, o, G);
-            const float dl = f.d * tr / (float)L;
+            // relative loading d*tr(R)/L, or an absolute d on the normalised R
+            const float dl = f.loading == COS_CAPON_LOAD_ABSOLUTE ? f.d * (float)(Ns * T) : f.d * tr / (float)L;
 #pragma unroll
             for (int m = 0; m < NM; ++m)
 #pragma unroll

@@ -66,6 +66,18 @@ int fused_candidates_l16_t5(const FusedCandidate **out);
 int fused_candidates_l32_t1(const FusedCandidate **out);
 int fused_candidates_l32_t3(const FusedCandidate **out);
 int fused_candidates_l32_t5(const FusedCandidate **out);
+// adjoint of the output power
+struct AdjDev {
+    const float2 *x;   // [Nx][Ny][M]
+    const float2 *w;   // [Nx][Npy][L]
+    const float *gP;   // [Nx][Npy]
+    float2 *gx;        // [Nx][Ny][M]   accumulated dloss/dconj(x)
+    float *gd;         // [1]           accumulated dloss/dd, or null
+    float *gth;        // [M]           accumulated dloss/dtheta, or null
+    int L, K, M, Nx, Ny, Npy;
+};
+
+int launch_adjoint(const AdjDev &a, int num_sms, cudaStream_t s);
 // beamspace path (Nb > 0)
 int launch_beamspace(const FrameDev &f, float2 *R_out, cudaStream_t s);
 int launch_butler(float2 *B, int Nb, int L, cudaStream_t s);

@@ -76,7 +76,8 @@ plain_build_r_kernel(FrameDev f, float2 *__restrict__ Rout, int ref_layout)
     }
     trace = __shfl_sync(0xffffffffu, trace, 0);
     __syncwarp();
-    const float dl = f.d * trace * norm / (float)L;
+    const float dl = f.loading == COS_CAPON_LOAD_ABSOLUTE ? f.d * (float)(Ns * T) * norm
+                                                          : f.d * trace * norm / (float)L;
     for (int k = lane; k < L; k += 32) Rp[(size_t)k * L + k].x += dl;
 }
 

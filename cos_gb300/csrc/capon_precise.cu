@@ -116,7 +116,7 @@ precise_build_r_kernel(FrameDev f, float2 *__restrict__ Rhi, float2 *__restrict_
         }
     }
     const float tr = __shfl_sync(0xffffffffu, trh + trl, 0);
-    if (lane == 0) dlo[pix] = f.d * tr / (float)L;
+    if (lane == 0) dlo[pix] = f.loading == COS_CAPON_LOAD_ABSOLUTE ? f.d * (float)(Ns * T) : f.d * tr / (float)L;
 }
 
 // One warp per pixel: FP32 Cholesky of R_hi + dl I in shared memory (row-major

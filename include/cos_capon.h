@@ -39,6 +39,8 @@ extern "C" {
                                        (reference GPU default, buildR_kernel.cu:153-154)          */
 #define COS_CAPON_LOAD_BEAMSPACE 1  /* load after the transform with tr(R_bs)/Nb
                                        (getCaponAllC.pyx:376-385; sliding route BuildR.cpp:82-86) */
+#define COS_CAPON_LOAD_ABSOLUTE  2  /* R_d = R + d*I on the normalised R: an absolute (e.g.
+                                       learnable) loading, the form the adjoint differentiates */
 
 #define COS_CAPON_R_REFERENCE  0  /* R as the reference GPU writes it: per pixel column-major,
                                      loaded, not normalised (buildR_kernel.cu:84-86,153-157)       */
@@ -95,8 +97,7 @@ int cos_capon_get_capon_ex(cos_capon_ctx *ctx, void *z, float *P, void *w, void 
                            int Nb, const cos_capon_opts *opts);
 
 /* Device-pointer call: every pixel of `nframes` frames (each with its own M, L,
- * K, Nb) in one launch on `stream` (a cudaStream_t, NULL = the context's
- * stream).  Asynchronous; no host synchronisation and no allocation once the
+ * K, Nb) in one launch on `stream` (a cudaStream_t; NULL = the default stream).  Asynchronous; no host synchronisation and no allocation once the
  * context has served a call of the same or larger shape, so it can be captured
  * into a CUDA graph after one warm-up call. */
 int cos_capon_run(cos_capon_ctx *ctx, const cos_capon_frame *frames, int nframes,
@@ -121,6 +122,29 @@ int cos_capon_solve(cos_capon_ctx *ctx, void *x, const void *A, const void *b, i
  * pointer (B_on_gpu): B[b,l] = exp(-j*2*pi*bin(b)*l/L)/sqrt(L) with the beam
  * layout of capon_kernel.cu:47-77 (butler_matrix). */
 int cos_capon_butler(cos_capon_ctx *ctx, void *B, int Nb, int L, int B_on_gpu);
+
+/* Adjoint of the output power (no counterpart in the reference; the
+ * differentiable path).  For a loss l(P) with per-pixel gradient gP = dl/dP of
+ * a forward call with absolute loading R_d = R + d I (COS_CAPON_LOAD_ABSOLUTE),
+ * accumulates
+ *   gx[b][y][m]  += dl/dconj(x[b][y][m])                  (complex64)
+ *   gd[0]        += dl/dd                                   (float32, or NULL)
+ *   gtheta[m]    += dl/dtheta_m for inputs x_m exp(-j theta_m) (float32 [M], or NULL)
+ * from the cube x and the weights w of that forward call (dP = w^H dR_d w, so
+ * neither R nor its factor is stored or rebuilt).  Pixels with gP = 0 are
+ * skipped.  The caller zeroes the accumulators.  Device pointers, asynchronous;
+ * element space, L <= 64. */
+typedef struct cos_capon_adjoint {
+    const void *x;    /* device, complex64 [Nx][Ny][M]        */
+    const void *w;    /* device, complex64 [Nx][Ny-2K][L]     */
+    const float *gP;  /* device, float32   [Nx][Ny-2K]        */
+    void *gx;         /* device, complex64 [Nx][Ny][M]        */
+    float *gd;        /* device, float32   [1]  or NULL       */
+    float *gtheta;    /* device, float32   [M]  or NULL       */
+    int L, K, M, Nx, Ny;
+} cos_capon_adjoint;
+
+int cos_capon_backward(cos_capon_ctx *ctx, const cos_capon_adjoint *adj, void *stream);  /* NULL = default stream */
 
 /* Status word of the last launch on this context (0, or COS_CAPON_ERR_TIMEOUT
  * when a bounded device-side wait gave up).  Synchronises the context stream. */

@@ -36,6 +36,8 @@
  * (w = Ria / sum(Ria), z = sum conj(w) g; capon_kernel.cu:338-427).
  * `bs_loading = 1` instead loads after the transform with trace(R_bs)/Nb, the
  * convention of framework/beamformer/capon/getCaponAllC.pyx:376-385.
+ * `bs_loading = 2` adds an absolute loading regCoef*I to the normalised R (no
+ * reference counterpart: the form with a learnable loading scalar).
  */
 #define _GNU_SOURCE
 #include <complex.h>
@@ -204,7 +206,7 @@ static void pixel_run(const job_t *jb, int x, int y, cplx *scratch)
         /* :257-262 diagonal loading */
         cplx tr = 0;
         for (int i = 0; i < L; ++i) tr += R[i * L + i];
-        cplx dl = tr * regCoef / L;
+        cplx dl = jb->bs_loading == 2 ? (cplx)regCoef : tr * regCoef / L;
         for (int i = 0; i < L; ++i) R[i * L + i] += dl;
         for (int i = 0; i < L; ++i) a[i] = 1.0;
         /* :274 */
@@ -230,10 +232,10 @@ static void pixel_run(const job_t *jb, int x, int y, cplx *scratch)
         cplx *xb = ab + Nb;                            /* Nb */
         cplx *wb = xb + Nb;                            /* 2 Nb Nb + Nb */
         oracle_butler(Nb, L, B);
-        if (!jb->bs_loading) {
+        if (jb->bs_loading != 1) {
             cplx tr = 0;
             for (int i = 0; i < L; ++i) tr += R[i * L + i];
-            cplx dl = tr * regCoef / L;
+            cplx dl = jb->bs_loading == 2 ? (cplx)regCoef : tr * regCoef / L;
             for (int i = 0; i < L; ++i) R[i * L + i] += dl;
         }
         for (int b = 0; b < Nb; ++b)
@@ -248,7 +250,7 @@ static void pixel_run(const job_t *jb, int x, int y, cplx *scratch)
                 for (int l = 0; l < L; ++l) s += tmp[b * L + l] * conj(B[c * L + l]);
                 Rb[b * Nb + c] = s;
             }
-        if (jb->bs_loading) {   /* getCaponAllC.pyx:376-385 */
+        if (jb->bs_loading == 1) {   /* getCaponAllC.pyx:376-385 */
             cplx tr = 0;
             for (int i = 0; i < Nb; ++i) tr += Rb[i * Nb + i];
             cplx dl = tr * regCoef / Nb;

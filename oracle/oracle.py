@@ -57,7 +57,9 @@ def _p(a):
 
 
 def capon(Xd, regCoef, L, Navg, Nb=0, bs_loading=False, fp32_scalars=True, want_w=True, want_R=False,
-          nthreads=1) -> dict:
+          nthreads=1, absolute=False) -> dict:
+    """absolute=True: R_d = R + regCoef*I on the normalised R instead of the
+    relative loading regCoef*tr(R)/L."""
     Xd = np.ascontiguousarray(Xd, dtype=np.complex64)
     Nx, Ny, M = Xd.shape
     npy = Ny - 2 * Navg
@@ -68,7 +70,8 @@ def capon(Xd, regCoef, L, Navg, Nb=0, bs_loading=False, fp32_scalars=True, want_
         w=np.zeros((Nx, npy, L), np.complex128) if want_w else None,
         R=np.zeros((Nx, npy, L, L), np.complex128) if want_R else None,
     )
-    rc = lib().oracle_capon(_p(Xd), Nx, Ny, M, float(regCoef), int(L), int(Navg), int(Nb), int(bool(bs_loading)),
+    mode = 2 if absolute else int(bool(bs_loading))
+    rc = lib().oracle_capon(_p(Xd), Nx, Ny, M, float(regCoef), int(L), int(Navg), int(Nb), mode,
                             int(bool(fp32_scalars)), _p(out["z"]), _p(out["zpow"]), _p(out["w"]), _p(out["P"]),
                             _p(out["R"]), int(nthreads))
     if rc != 0:
