@@ -311,6 +311,43 @@ def run_gpu(args) -> None:
     except Exception as exc:  # reported, not fatal to the throughput line
         adj = {"error": str(exc)[:200]}
 
+    # config 2: four frames of uneven (M, L, Nb), one CUDA graph per step
+    cfg2 = None
+    try:
+        frames2 = []
+        npix2 = 0
+        for fr in synth.config2(seed=2):
+            x2 = torch.from_numpy(fr["x"]).cuda()
+            Nx2, Ny2, _ = fr["x"].shape
+            npy2 = Ny2 - 2 * fr["K"]
+            npix2 += Nx2 * npy2
+            frames2.append(capon.DeviceFrame(x=x2, L=fr["L"], K=fr["K"], d=fr["d"], Nb=fr["Nb"],
+                                             z=torch.empty((Nx2, npy2), dtype=torch.complex64, device="cuda"),
+                                             P=torch.empty((Nx2, npy2), dtype=torch.float32, device="cuda")))
+        with torch.cuda.stream(stream):
+            for _ in range(2):
+                capon.capon_frames(frames2, ctx, stream=stream)
+        stream.synchronize()
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, stream=stream):
+            capon.capon_frames(frames2, ctx, stream=stream)
+        for _ in range(args.warmup):
+            graph.replay()
+        torch.cuda.synchronize()
+        g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        g0.record()
+        for _ in range(args.steps):
+            graph.replay()
+        g1.record()
+        g1.synchronize()
+        ms2 = g0.elapsed_time(g1) / args.steps
+        cfg2 = {"workload": "4 frames [Ny=1024, Nx=256]: (M,L,Nb) = (32,16,0), (64,32,0), (96,48,3), (128,64,5), K=1",
+                "pixels_per_step": npix2, "ms_per_step": ms2, "pixels_per_s": npix2 / (ms2 * 1e-3),
+                "launch": "one CUDA graph replay per step"}
+        del frames2
+    except Exception as exc:
+        cfg2 = {"error": str(exc)[:200]}
+
     # parity of this very run against the FP64 oracle on sampled beams
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle  # noqa: E402
@@ -349,6 +386,7 @@ def run_gpu(args) -> None:
                          "bytes_per_pixel": BYTES_PER_PIXEL, "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
         "clocks": clocks,
         "adjoint": adj,
+        "config2": cfg2,
     }
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = {k: v for k, v in cpu_reference_rate(os.cpu_count() or 1, 16).items()

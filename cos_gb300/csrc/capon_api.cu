@@ -60,6 +60,8 @@ struct cos_capon_ctx {
     // autotuner: chosen fused candidate per (L, K, M, w-or-R requested)
     std::map<std::tuple<int, int, int, int>, int> tuned;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // second stream of the pipelined host-pointer call
+    cudaStream_t stream2 = nullptr;
 };
 
 static const cos_capon_opts kDefaultOpts = {COS_CAPON_FORM_FUSED, COS_CAPON_LOAD_ELEMENT, COS_CAPON_R_REFERENCE, 0};
@@ -279,6 +281,16 @@ static int run_frames(cos_capon_ctx *c, const FrameDev *fs, int n, const cos_cap
     return 0;
 }
 
+static bool is_pinned(const void *p)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
 static int read_status(cos_capon_ctx *c, cudaStream_t s, bool sync)
 {
     if (sync) {
@@ -328,6 +340,7 @@ int cos_capon_destroy(cos_capon_ctx *c)
         b->release();
     if (c->d_status) cudaFree(c->d_status);
     if (c->stream) cudaStreamDestroy(c->stream);
+    if (c->stream2) cudaStreamDestroy(c->stream2);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     delete c;
@@ -389,8 +402,59 @@ int cos_capon_get_capon_ex(cos_capon_ctx *c, void *z, float *P, void *w, void *R
     if (R && (e = c->R.ensure(bR))) return e;
 
     cudaStream_t s = c->stream;
-    cudaError_t ce = cudaMemcpyAsync(c->x.p, x, bx, cudaMemcpyHostToDevice, s);
-    if (ce != cudaSuccess) return ce;
+    cudaError_t ce;
+    // Pinned host buffers and a path without shared scratch (fused, beamspace):
+    // split the beams into chunks on two streams so that the copies of one
+    // chunk overlap the kernel of the other.  The first call of a fused shape
+    // runs whole, so the autotuner times the frame once, on one stream.
+    const bool fused = use_fused(make_frame(probe, o), o);
+    const bool no_scratch = fused || Nb > 0;
+    const bool tuned = !fused || c->tuned.count(std::make_tuple(L, Yavg, M, (int)(w != nullptr || R != nullptr)));
+    if (no_scratch && tuned && !R && Nx >= 4 && is_pinned(x) && is_pinned(z) && (!P || is_pinned(P)) &&
+        (!w || is_pinned(w))) {
+        if (!c->stream2 && cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking) != cudaSuccess) {
+            cudaGetLastError();
+            c->stream2 = nullptr;
+        }
+        if (c->stream2) {
+            const int nch = Nx >= 16 ? 8 : Nx / 2;
+            const size_t rowx = (size_t)Nz * M, rowp = (size_t)(Nz - 2 * Yavg);
+            for (int ch = 0; ch < nch; ++ch) {
+                const int b0 = (int)((long)Nx * ch / nch), b1 = (int)((long)Nx * (ch + 1) / nch);
+                cudaStream_t sc = (ch & 1) ? c->stream2 : c->stream;
+                const size_t nb = (size_t)(b1 - b0);
+                if ((ce = cudaMemcpyAsync((float2 *)c->x.p + b0 * rowx, (const float2 *)x + b0 * rowx,
+                                          nb * rowx * sizeof(float2), cudaMemcpyHostToDevice, sc)) != cudaSuccess)
+                    return ce;
+                cos_capon_frame fr;
+                memset(&fr, 0, sizeof(fr));
+                fr.x = (float2 *)c->x.p + b0 * rowx;
+                fr.z = (float2 *)c->z.p + b0 * rowp;
+                fr.P = P ? (float *)c->P.p + b0 * rowp : nullptr;
+                fr.w = w ? (float2 *)c->w.p + b0 * rowp * L : nullptr;
+                fr.d = d;
+                fr.L = L;
+                fr.K = Yavg;
+                fr.M = M;
+                fr.Nx = (int)nb;
+                fr.Ny = Nz;
+                fr.Nb = Nb;
+                if ((e = cos_capon_run(c, &fr, 1, &o, sc))) return e;
+                if ((ce = cudaMemcpyAsync((float2 *)z + b0 * rowp, fr.z, nb * rowp * sizeof(float2),
+                                          cudaMemcpyDeviceToHost, sc)) != cudaSuccess)
+                    return ce;
+                if (P && (ce = cudaMemcpyAsync(P + b0 * rowp, fr.P, nb * rowp * sizeof(float), cudaMemcpyDeviceToHost,
+                                               sc)) != cudaSuccess)
+                    return ce;
+                if (w && (ce = cudaMemcpyAsync((float2 *)w + b0 * rowp * L, fr.w, nb * rowp * L * sizeof(float2),
+                                               cudaMemcpyDeviceToHost, sc)) != cudaSuccess)
+                    return ce;
+            }
+            if ((ce = cudaStreamSynchronize(c->stream2)) != cudaSuccess) return ce;
+            return read_status(c, s, true);
+        }
+    }
+    if ((ce = cudaMemcpyAsync(c->x.p, x, bx, cudaMemcpyHostToDevice, s)) != cudaSuccess) return ce;
     cos_capon_frame fr;
     fr.x = c->x.p;
     fr.z = c->z.p;

@@ -273,3 +273,59 @@ def test_refinement_option_on_fused_shape(cap):
                                   cap.opts(refine=1)) == 0
     ref = oracle.capon(x, c["d"], c["L"], c["K"], want_w=False, nthreads=3)
     assert np.max(np.abs(P - ref["P"]) / ref["P"]) <= 1e-6
+
+
+def test_pinned_host_buffers_pipelined(cap):
+    """Pinned host buffers take the chunked two-stream path of
+    cos_capon_get_capon_ex; its outputs equal the unpinned single-chunk call."""
+    import torch
+    from cos_gb300 import synth
+    c = synth.config1(seed=5, Nx=16, Ny=256)
+    x = c["x"]
+    Nx, Ny, M = x.shape
+    npy = Ny - 2 * c["K"]
+    ctx = cap.Capon()
+    z0 = np.zeros((Nx, npy), np.complex64)
+    P0 = np.zeros((Nx, npy), np.float32)
+    assert ctx.getCaponEx(z0, P0, None, None, x, c["d"], c["L"], c["K"], M, Nx, Ny, 0) == 0   # tunes
+    xp = torch.from_numpy(x).pin_memory()
+    zp = torch.zeros((Nx, npy), dtype=torch.complex64).pin_memory()
+    Pp = torch.zeros((Nx, npy), dtype=torch.float32).pin_memory()
+    for _ in range(2):
+        assert ctx.getCaponEx(zp.numpy(), Pp.numpy(), None, None, xp.numpy(), c["d"], c["L"], c["K"], M, Nx, Ny,
+                              0) == 0
+        np.testing.assert_array_equal(zp.numpy(), z0)
+        np.testing.assert_array_equal(Pp.numpy(), P0)
+
+
+def test_multi_frame_cuda_graph(cap):
+    """The config-2 frames (uneven M, L, Nb) captured as one CUDA graph and
+    replayed: the replay reproduces the eager call."""
+    import torch
+    from cos_gb300 import synth
+    cfg = synth.config2(seed=2, Ny=64, Nx=4)
+    ctx = cap.Context()
+    frames = []
+    for fr in cfg:
+        xt = torch.from_numpy(fr["x"]).cuda()
+        Nx, Ny, M = fr["x"].shape
+        npy = Ny - 2 * fr["K"]
+        frames.append(cap.DeviceFrame(x=xt, L=fr["L"], K=fr["K"], d=fr["d"], Nb=fr["Nb"],
+                                      z=torch.empty((Nx, npy), dtype=torch.complex64, device="cuda"),
+                                      P=torch.empty((Nx, npy), dtype=torch.float32, device="cuda")))
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        cap.capon_frames(frames, ctx, stream=s)            # eager: tunes, sizes buffers
+    s.synchronize()
+    eager = [(f.z.clone(), f.P.clone()) for f in frames]
+    for f in frames:
+        f.z.zero_()
+        f.P.zero_()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        cap.capon_frames(frames, ctx, stream=s)
+    for _ in range(2):
+        g.replay()
+        torch.cuda.synchronize()
+        for f, (z0, P0) in zip(frames, eager):
+            assert torch.equal(f.z, z0) and torch.equal(f.P, P0)
