@@ -18,7 +18,7 @@ ERR_LAUNCH = 719
 ERR_NOT_SUPPORTED = 801
 ERR_TIMEOUT = 909
 
-FORM_FUSED, FORM_PLAIN = 0, 1
+FORM_FUSED, FORM_PLAIN, FORM_TC_TF32, FORM_TC_BF16X3, FORM_TC_TF32X3 = 0, 1, 2, 3, 4
 LOAD_ELEMENT, LOAD_BEAMSPACE, LOAD_ABSOLUTE = 0, 1, 2
 R_REFERENCE, R_NORMALISED = 0, 1
 

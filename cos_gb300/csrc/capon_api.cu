@@ -236,12 +236,39 @@ static int run_precise(cos_capon_ctx *c, FrameDev f, bool refine, cudaStream_t s
     if ((e = launch_precise(f, (float2 *)c->Rwork.p, (float2 *)c->Rlo.p, (float *)c->dl.p, (float2 *)c->Ria.p,
                             c->d_status, refine, s)))
         return e;
-    if (f.R) e = launch_plain_build_r(f, f.R, f.r_layout == COS_CAPON_R_REFERENCE ? 1 : 0, s);
+    // the requested R is the float-float matrix the solve used, plus the loading
+    if (f.R) e = launch_format_r(f, (float2 *)c->Rwork.p, (float2 *)c->Rlo.p, (float *)c->dl.p, f.R, s);
+    return e;
+}
+
+static bool is_tc_form(int form)
+{
+    return form == COS_CAPON_FORM_TC_TF32 || form == COS_CAPON_FORM_TC_BF16X3 || form == COS_CAPON_FORM_TC_TF32X3;
+}
+
+// tensor-core covariance form: tcgen05 window Gram + float-float smoothing ->
+// FP32 Cholesky (+ FP64-residual refinement) -> outputs
+static int run_tc(cos_capon_ctx *c, FrameDev f, int split, bool refine, cudaStream_t s)
+{
+    const size_t npix = (size_t)f.Nx * f.Npy;
+    int e;
+    if ((e = c->Rwork.ensure(npix * f.L * f.L * sizeof(float2)))) return e;
+    if ((e = c->dl.ensure(npix * sizeof(float)))) return e;
+    if ((e = c->Ria.ensure(npix * f.L * sizeof(float2)))) return e;
+    float2 *Rw = (float2 *)c->Rwork.p;
+    float *dl = (float *)c->dl.p;
+    if ((e = launch_tc_covariance(f, split, Rw, dl, c->d_status, c->num_sms, s))) return e;
+    if ((e = launch_precise_solve(f, Rw, nullptr, dl, (float2 *)c->Ria.p, c->d_status, refine, s))) return e;
+    if (f.R) e = launch_format_r(f, Rw, nullptr, dl, f.R, s);
     return e;
 }
 
 static int run_frames(cos_capon_ctx *c, const FrameDev *fs, int n, const cos_capon_opts &o, cudaStream_t s)
 {
+    if (o.form < COS_CAPON_FORM_FUSED || o.form > COS_CAPON_FORM_TC_TF32X3) return COS_CAPON_ERR_NOT_SUPPORTED;
+    if (is_tc_form(o.form))
+        for (int k = 0; k < n; ++k)
+            if (fs[k].Nb != 0 || !tc_supported(fs[k], o.form)) return COS_CAPON_ERR_NOT_SUPPORTED;
     // batch consecutive fused frames with equal (L, K, M) into one launch
     int i = 0;
     while (i < n) {
@@ -272,8 +299,9 @@ static int run_frames(cos_capon_ctx *c, const FrameDev *fs, int n, const cos_cap
         } else {
             // element space without a fused instantiation (or with refinement):
             // the precise pipeline; the plain form when asked for
-            int e = (o.form == COS_CAPON_FORM_PLAIN && !o.refine) ? run_plain(c, f, s)
-                                                                  : run_precise(c, f, o.refine != 0, s);
+            int e = is_tc_form(o.form)                          ? run_tc(c, f, o.form, o.refine != 0, s)
+                    : (o.form == COS_CAPON_FORM_PLAIN && !o.refine) ? run_plain(c, f, s)
+                                                                    : run_precise(c, f, o.refine != 0, s);
             if (e) return e;
             ++i;
         }

@@ -48,6 +48,18 @@ int launch_plain_output(const FrameDev &f, const float2 *Ria, cudaStream_t s);
 // optional FP64-residual refinement); Rhi/Rlo hold Nx*Npy*L*L, dl Nx*Npy, Ria Nx*Npy*L
 int launch_precise(const FrameDev &f, float2 *Rhi, float2 *Rlo, float *dl, float2 *Ria, unsigned *status,
                    bool refine, cudaStream_t s);
+// FP32 Cholesky solve (optionally refined with an FP64 residual against
+// Rhi + Rlo + dl; Rlo may be null) and the output stage
+int launch_precise_solve(const FrameDev &f, const float2 *Rhi, const float2 *Rlo, const float *dl, float2 *Ria,
+                         unsigned *status, bool refine, cudaStream_t s);
+// Rhi (+ Rlo) plus the loading dl written in the frame's R layout
+int launch_format_r(const FrameDev &f, const float2 *Rhi, const float2 *Rlo, const float *dl, float2 *out,
+                    cudaStream_t s);
+// tensor-core covariance (tcgen05, TMEM): Rw = R per pixel (column-major, not
+// normalised, not loaded) and dl, for split = COS_CAPON_FORM_TC_*
+bool tc_supported(const FrameDev &f, int split);
+int launch_tc_covariance(const FrameDev &f, int split, float2 *Rw, float *dl, unsigned *status, int num_sms,
+                         cudaStream_t s);
 // general batched LU solve, column-major A
 int launch_lu_solve(float2 *x, const float2 *A, const float2 *b, int N, int batch, cudaStream_t s);
 // fused element-space path: candidate configurations per subarray length.

@@ -133,7 +133,7 @@ precise_solve_kernel(int L, long long batch, const float2 *__restrict__ Rhi, con
     const int ld = L + 1;
     float2 *A = smem + (size_t)warp * (L * ld + 2 * L);
     float2 *xb = A + (size_t)L * ld;   // x0 broadcast buffer
-    const float2 *Rh = Rhi + (size_t)sys * L * L, *Rl = Rlo + (size_t)sys * L * L;
+    const float2 *Rh = Rhi + (size_t)sys * L * L, *Rl = Rlo ? Rlo + (size_t)sys * L * L : nullptr;
     const float dl = dlv[sys];
     for (int i = lane; i < L * L; i += 32) {
         const int a = i % L, b = i / L;
@@ -191,7 +191,8 @@ precise_solve_kernel(int L, long long batch, const float2 *__restrict__ Rhi, con
             double rr = 1.0, ri = 0.0;
             if (i < L) {
                 for (int j = 0; j < L; ++j) {
-                    const float2 h = Rh[i + (size_t)j * L], l = Rl[i + (size_t)j * L], xj = xb[j];
+                    const float2 h = Rh[i + (size_t)j * L], xj = xb[j];
+                    const float2 l = Rlo ? Rl[i + (size_t)j * L] : make_float2(0.f, 0.f);
                     const double ar = (double)h.x + (double)l.x + (i == j ? (double)dl : 0.0);
                     const double ai = (double)h.y + (double)l.y;
                     rr -= ar * (double)xj.x - ai * (double)xj.y;
@@ -209,22 +210,45 @@ precise_solve_kernel(int L, long long batch, const float2 *__restrict__ Rhi, con
     if (bad && lane == 0) atomicOr(status, ERR_NOT_PD);
 }
 
-int launch_precise(const FrameDev &f, float2 *Rhi, float2 *Rlo, float *dl, float2 *Ria, unsigned *status,
-                   bool refine, cudaStream_t s)
+// R of the pipeline (R_hi + R_lo, column-major, not normalised) plus the
+// loading, in the caller's layout: the reference's (column-major, loaded, not
+// normalised) or row-major, loaded and normalised by 1/(Ns T)
+__global__ void format_r_kernel(long long n, int L, float scale, int ref_layout, const float2 *__restrict__ Rhi,
+                                const float2 *__restrict__ Rlo, const float *__restrict__ dlv, float2 *__restrict__ out)
+{
+    const long long L2 = (long long)L * L;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n * L2;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long pix = i / L2;
+        const int e = (int)(i % L2), a = e % L, b = e / L;   // source element (a, b), column-major
+        float2 v = Rhi[i];
+        if (Rlo) v = fadd2(v, Rlo[i]);
+        if (a == b) v.x += dlv[pix];
+        v = cscale(v, scale);
+        out[pix * L2 + (ref_layout ? e : a * L + b)] = v;
+    }
+}
+
+int launch_format_r(const FrameDev &f, const float2 *Rhi, const float2 *Rlo, const float *dl, float2 *out,
+                    cudaStream_t s)
 {
     const long long npix = (long long)f.Nx * f.Npy;
-    const size_t sm1 = (size_t)kPrecWarps * (2 * f.K + 1) * f.M * sizeof(float2);
+    const int ref = f.r_layout == COS_CAPON_R_REFERENCE;
+    const float scale = ref ? 1.f : 1.f / ((float)(f.M - f.L + 1) * (float)(2 * f.K + 1));
+    long long blocks = (npix * f.L * f.L + 255) / 256;
+    if (blocks > 152 * 64) blocks = 152 * 64;
+    format_r_kernel<<<(unsigned)blocks, 256, 0, s>>>(npix, f.L, scale, ref, Rhi, Rlo, dl, out);
+    return cudaGetLastError();
+}
+
+int launch_precise_solve(const FrameDev &f, const float2 *Rhi, const float2 *Rlo, const float *dl, float2 *Ria,
+                         unsigned *status, bool refine, cudaStream_t s)
+{
+    const long long npix = (long long)f.Nx * f.Npy;
     const size_t sm2 = (size_t)kPrecWarps * (f.L * (f.L + 1) + 2 * f.L) * sizeof(float2);
-    if (sm1 > 227 * 1024 || sm2 > 227 * 1024 || f.L > 64) return cudaErrorNotSupported;
-    cudaError_t e;
+    if (sm2 > 227 * 1024 || f.L > 64) return cudaErrorNotSupported;
     const long long blocks = (npix + kPrecWarps - 1) / kPrecWarps;
-    // exact products always: this pipeline serves the stress cases (L = 48, 64,
-    // light loading) and the refinement option, where the covariance's own
-    // rounding is what limits the power accuracy
-    e = cudaFuncSetAttribute(precise_build_r_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
-    if (e != cudaSuccess) return e;
-    precise_build_r_kernel<true><<<(unsigned)blocks, 32 * kPrecWarps, sm1, s>>>(f, Rhi, Rlo, dl);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    cudaError_t e;
     if (refine) {
         e = cudaFuncSetAttribute(precise_solve_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
         if (e != cudaSuccess) return e;
@@ -236,6 +260,24 @@ int launch_precise(const FrameDev &f, float2 *Rhi, float2 *Rlo, float *dl, float
     }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     return launch_plain_output(f, Ria, s);
+}
+
+int launch_precise(const FrameDev &f, float2 *Rhi, float2 *Rlo, float *dl, float2 *Ria, unsigned *status,
+                   bool refine, cudaStream_t s)
+{
+    const long long npix = (long long)f.Nx * f.Npy;
+    const size_t sm1 = (size_t)kPrecWarps * (2 * f.K + 1) * f.M * sizeof(float2);
+    if (sm1 > 227 * 1024 || f.L > 64) return cudaErrorNotSupported;
+    cudaError_t e;
+    const long long blocks = (npix + kPrecWarps - 1) / kPrecWarps;
+    // exact products always: this pipeline serves the stress cases (L = 48, 64,
+    // light loading) and the refinement option, where the covariance's own
+    // rounding is what limits the power accuracy
+    e = cudaFuncSetAttribute(precise_build_r_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
+    if (e != cudaSuccess) return e;
+    precise_build_r_kernel<true><<<(unsigned)blocks, 32 * kPrecWarps, sm1, s>>>(f, Rhi, Rlo, dl);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    return launch_precise_solve(f, Rhi, Rlo, dl, Ria, status, refine, s);
 }
 
 }  // namespace cgb

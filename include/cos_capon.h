@@ -34,6 +34,13 @@ extern "C" {
 /* ---- options ------------------------------------------------------------ */
 #define COS_CAPON_FORM_FUSED   0  /* one fused persistent kernel per launch (default)             */
 #define COS_CAPON_FORM_PLAIN   1  /* plain FP32 three-stage pipeline: build R -> solve -> output   */
+/* Tensor-core covariance (element space, M a multiple of 16 up to 128, L <= 64):
+   the window Gram on tcgen05 in the named operand precision, smoothing in
+   float-float, then the FP32 Cholesky (with refine=1 one FP64-residual step).
+   No reference counterpart; precision forms for comparison against FP64.      */
+#define COS_CAPON_FORM_TC_TF32   2  /* TF32 operands (rna), FP32 accumulation           */
+#define COS_CAPON_FORM_TC_BF16X3 3  /* BF16 hi/lo split, three products, FP32 accum.    */
+#define COS_CAPON_FORM_TC_TF32X3 4  /* TF32 hi/lo split, three products, FP32 accum.    */
 
 #define COS_CAPON_LOAD_ELEMENT   0  /* R_d = R + d*tr(R)/L*I before any beamspace transform
                                        (reference GPU default, buildR_kernel.cu:153-154)          */

@@ -1,0 +1,112 @@
+"""Tensor-core covariance forms (tcgen05 window Gram, float-float smoothing,
+FP32 Cholesky) against the FP64 oracle.
+
+Tolerances are per operand precision and hold for the seeded cubes below
+(scatterers 20 dB above the noise; the stress case two coherent scatterers at
+40 dB with light loading).  R is compared as max|dR| / max|R|, P per pixel.
+  TF32    (10-bit operands)           R 1e-3, P 1e-2
+  BF16x3  (16-bit split, 3 products)  R 2e-5, P 1e-2
+  TF32x3  (22-bit split, 3 products)  R 1e-6, P 1e-4 (stress case 1e-3)
+"""
+import numpy as np
+import pytest
+
+from cos_gb300 import _lib, synth
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+FORMS = {"tf32": _lib.FORM_TC_TF32, "bf16x3": _lib.FORM_TC_BF16X3, "tf32x3": _lib.FORM_TC_TF32X3}
+TOL_R = {"tf32": 1e-3, "bf16x3": 2e-5, "tf32x3": 1e-6}
+TOL_P = {"tf32": 1e-2, "bf16x3": 1e-2, "tf32x3": 1e-4}
+
+SHAPES = [  # M, L, K, loading
+    (64, 32, 2, 0.01),
+    (32, 16, 1, 0.01),
+    (48, 24, 1, 0.01),   # 96 of the 128 accumulator lanes used
+    (16, 8, 0, 0.01),    # eight pixels per MMA, K = 0
+    (128, 64, 4, 1e-3),  # the precision stress shape
+]
+
+
+@pytest.fixture(scope="module")
+def cap():
+    from cos_gb300 import capon
+    return capon
+
+
+def _cube(M, K, Nx=3):
+    Ny = 24 + 2 * K
+    stress = M == 128
+    return synth.cube(Ny, Nx, M, [100.0, 100.0] if stress else [10.0, 5.0], M, coherent_pair=stress)
+
+
+def _run(cap, x, d, L, K, form, refine=0):
+    Nx, Ny, M = x.shape
+    npy = Ny - 2 * K
+    z = np.zeros((Nx, npy), np.complex64)
+    P = np.zeros((Nx, npy), np.float32)
+    w = np.zeros((Nx, npy, L), np.complex64)
+    R = np.zeros((Nx, npy, L, L), np.complex64)
+    o = cap.opts(form=form, r_layout=_lib.R_NORMALISED, refine=refine)
+    ctx = cap.Capon()
+    assert ctx.getCaponEx(z, P, w, R, x, d, L, K, M, Nx, Ny, 0, o) == 0
+    return z, P, w, R
+
+
+@pytest.mark.parametrize("name", list(FORMS))
+@pytest.mark.parametrize("M,L,K,d", SHAPES)
+def test_tc_form_matches_fp64(cap, name, M, L, K, d):
+    x = _cube(M, K)
+    ref = oracle.capon(x, d, L, K, want_R=True, want_w=True, nthreads=8)
+    z, P, w, R = _run(cap, x, d, L, K, FORMS[name])
+    eR = np.abs(R - ref["R"]).max() / np.abs(ref["R"]).max()
+    eP = (np.abs(P - ref["P"]) / ref["P"]).max()
+    ez = (np.abs(z - ref["z"]) / np.abs(ref["z"]).max()).max()
+    print(f"M{M} L{L} K{K} {name}: R {eR:.2e} P {eP:.2e} z {ez:.2e}")
+    assert eR < TOL_R[name]
+    assert eP < (1e-3 if (name == "tf32x3" and M == 128) else TOL_P[name])
+
+
+def test_tc_refine_and_repeat(cap):
+    """With refine=1 the FP64 residual runs against the form's own R; repeated
+    calls give identical outputs (no state carried between launches)."""
+    x = _cube(64, 2, Nx=4)
+    ref = oracle.capon(x, 0.01, 32, 2, nthreads=8)
+    a = _run(cap, x, 0.01, 32, 2, _lib.FORM_TC_TF32X3, refine=1)
+    b = _run(cap, x, 0.01, 32, 2, _lib.FORM_TC_TF32X3, refine=1)
+    for u, v in zip(a, b):
+        np.testing.assert_array_equal(u, v)
+    assert (np.abs(a[1] - ref["P"]) / ref["P"]).max() < 1e-4
+
+
+def test_tc_forms_reject_unsupported_shapes(cap):
+    """M not a multiple of 16, M > 128 and beamspace frames are outside the
+    forms: COS_CAPON_ERR_NOT_SUPPORTED, nothing launched."""
+    ctx = cap.Capon()
+    for (M, L, Nb) in [(40, 16, 0), (144, 32, 0), (64, 32, 3)]:
+        x = np.zeros((2, 20, M), np.complex64)
+        z = np.zeros((2, 18), np.complex64)
+        P = np.zeros((2, 18), np.float32)
+        e = ctx.getCaponEx(z, P, None, None, x, 0.01, L, 1, M, 2, 20, Nb, cap.opts(form=_lib.FORM_TC_TF32))
+        assert e == _lib.ERR_NOT_SUPPORTED, (M, L, Nb, e)
+    x = np.zeros((2, 20, 32), np.complex64)
+    assert ctx.getCaponEx(z, P, None, None, x, 0.01, 16, 1, 32, 2, 20, 0, cap.opts(form=7)) == _lib.ERR_NOT_SUPPORTED
+
+
+def test_tc_full_frame_properties(cap):
+    """Config-1 size through the device API: finite, positive power, and the
+    beams sampled from the full frame equal the same beams run alone."""
+    import torch
+    c = synth.config1(seed=1, Nx=64)
+    x = c["x"]
+    Nx, Ny, M = x.shape
+    xt = torch.from_numpy(x).cuda()
+    fr = cap.DeviceFrame(x=xt, L=32, K=2, d=0.01, P=torch.empty((Nx, Ny - 4), device="cuda"))
+    cap.capon_frames([fr], None, cap.opts(form=_lib.FORM_TC_BF16X3))
+    torch.cuda.synchronize()
+    P = fr.P.cpu().numpy()
+    assert np.isfinite(P).all() and (P > 0).all()
+    sub = np.ascontiguousarray(x[[0, 31, 63]])
+    _, Ps, _, _ = _run(cap, sub, 0.01, 32, 2, _lib.FORM_TC_BF16X3)
+    np.testing.assert_array_equal(Ps, P[[0, 31, 63]])
