@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 from cos_gb300 import _lib, synth
-from oracle import oracle
+import oracle
 
 pytestmark = pytest.mark.gpu
 
