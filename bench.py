@@ -48,6 +48,10 @@ EXEC_FLOP_PER_PIXEL = (8 * 2 * T * (L * (L + 1) // 2 - L) + 8 * NS * L + 2 * NS 
                        + (4.0 / 3.0) * L ** 3 + 2 * 8 * L * L / 2 * 2 + 16 * L)
 # Algorithmic HBM bytes per pixel: the cube once (8 M Ny/(Ny-2K)) + z + P.
 BYTES_PER_PIXEL = 8 * M * NY / (NY - 2 * K) + 8 + 4
+# DRAM bytes per pixel of the fused kernel from one ncu capture (dram__bytes_read
+# + dram__bytes_write = 174.05 MB over 327,040 pixels, the 160-beam profiling
+# case), scaled to a full launch by the pixels it processes.
+TRAFFIC_PER_PIXEL = 174.051072e6 / 327040
 CONFIG = {"workload": "capon-element-space M=64 L=32 K=2 [Nx=256,Ny=2048]", "M": M, "L": L, "K": K,
           "Nx": NX, "Ny": NY, "pixels_per_step": NPIX, "loading": D, "outputs": "z,P",
           "l2": "inputs larger than L2 (268 MB cube vs 126 MB L2)", "parallelism": "replicas"}
@@ -348,6 +352,13 @@ def run_gpu(args) -> None:
     except Exception as exc:
         cfg2 = {"error": str(exc)[:200]}
 
+    precision = None
+    if not args.no_precision and rank == 0:
+        try:
+            precision = precision_study(ctx, stream)
+        except Exception as exc:
+            precision = {"error": str(exc)[:200]}
+
     # parity of this very run against the FP64 oracle on sampled beams
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle  # noqa: E402
@@ -376,7 +387,8 @@ def run_gpu(args) -> None:
                 "h2d_bytes_per_step": int(x_host.nbytes), "d2h_bytes_per_step": int(zn.nbytes + Pn.nbytes)},
         "gpu_launches": args.steps,
         "roofline": {"bound": "fp32", "achieved": achieved_tf, "peak": fp32, "unit": "TFLOP/s",
-                     "frac": achieved_tf / fp32, "traffic": None,
+                     "frac": achieved_tf / fp32, "traffic": TRAFFIC_PER_PIXEL * NPIX, "traffic_unit": "bytes",
+                     "traffic_source": "ncu dram__bytes_read+write of the 160-beam case, scaled by pixels",
                      "peak_source": "measured here: cuBLAS FP32 SGEMM 8192^3, TF32 off",
                      "flop_per_pixel": FLOP_PER_PIXEL,
                      "executed_flop_per_pixel": EXEC_FLOP_PER_PIXEL, "executed_tflops": exec_tf,
@@ -387,6 +399,7 @@ def run_gpu(args) -> None:
         "clocks": clocks,
         "adjoint": adj,
         "config2": cfg2,
+        "precision": precision,
     }
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = {k: v for k, v in cpu_reference_rate(os.cpu_count() or 1, 16).items()
@@ -397,8 +410,73 @@ def run_gpu(args) -> None:
         dist.destroy_process_group()
 
 
+PRECISION_FORMS = [  # name, form, refine
+    ("all_fp32", 1, 0),                       # plain FP32 pipeline, the reference GPU algorithm
+    ("ff_cov_fp32_chol", 0, 0),               # float-float covariance, FP32 Cholesky
+    ("ff_cov_fp32_chol_fp64_refine", 1, 1),   # ... plus one FP64-residual refinement step
+    ("tc_tf32", 2, 0), ("tc_tf32_refine", 2, 1),
+    ("tc_bf16x3", 3, 0), ("tc_bf16x3_refine", 3, 1),
+    ("tc_tf32x3", 4, 0), ("tc_tf32x3_refine", 4, 1),
+]
+
+
+def precision_study(ctx, stream) -> dict:
+    """Precision stress workload: per-pixel relative errors of R, w and P for
+    every form against the FP64 oracle on the three beams with the most energy
+    (the coherent pair), and each form's time on the full frame."""
+    import torch
+    from cos_gb300 import _lib, capon, synth
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle  # noqa: E402
+    c = synth.config3(seed=3)
+    x, L, K, d = c["x"], c["L"], c["K"], c["d"]
+    Nx, Ny, M = x.shape
+    npy = Ny - 2 * K
+    beams = sorted(np.argsort(np.sum(np.abs(x) ** 2, axis=(1, 2)))[-3:].tolist())
+    sub = np.ascontiguousarray(x[beams])
+    ref = oracle.capon(sub, d, L, K, want_R=True, want_w=True, nthreads=os.cpu_count() or 1)
+    Rn = np.abs(ref["R"]).reshape(len(beams), npy, -1).max(-1)
+    wn = np.linalg.norm(ref["w"], axis=-1)
+    xt = torch.from_numpy(x).cuda()
+    cap = capon.Capon()
+    out = {"workload": f"[Nx={Nx}][Ny={Ny}][M={M}] L={L} K={K} loading {d}, two coherent scatterers 40 dB",
+           "error_sample": f"beams {beams} ({len(beams) * npy} pixels) vs FP64 oracle; R as max|dR|/max|R| per "
+                           "pixel, w as |dw|/|w|, P as |dP|/P", "forms": {}}
+    for name, form, refine in PRECISION_FORMS:
+        z = np.zeros((len(beams), npy), np.complex64)
+        P = np.zeros((len(beams), npy), np.float32)
+        w = np.zeros((len(beams), npy, L), np.complex64)
+        R = np.zeros((len(beams), npy, L, L), np.complex64)
+        o = capon.opts(form=form, r_layout=_lib.R_NORMALISED, refine=refine)
+        e = cap.getCaponEx(z, P, w, R, sub, d, L, K, M, len(beams), Ny, 0, o)
+        if e:
+            out["forms"][name] = {"status": e}
+            continue
+        eR = np.abs(R - ref["R"]).reshape(len(beams), npy, -1).max(-1) / Rn
+        ew = np.linalg.norm(w - ref["w"], axis=-1) / wn
+        eP = np.abs(P - ref["P"]) / ref["P"]
+        fr = capon.DeviceFrame(x=xt, L=L, K=K, d=d, P=torch.empty((Nx, npy), device="cuda"))
+        with torch.cuda.stream(stream):
+            capon.capon_frames([fr], ctx, o, stream)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(2):
+                capon.capon_frames([fr], ctx, o, stream)
+            e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / 2
+        out["forms"][name] = {"R_max": float(eR.max()), "R_median": float(np.median(eR)),
+                              "w_max": float(ew.max()), "w_median": float(np.median(ew)),
+                              "P_max": float(eP.max()), "P_median": float(np.median(eP)),
+                              "ms_full_frame": ms, "pixels_per_s": Nx * npy / (ms * 1e-3)}
+        del fr
+    del xt
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_profile_case(args) -> None:
-    """The fused kernel alone on Nx=profile_nx beams (for ncu captures)."""
+    """One form (default: fused) alone on Nx=profile_nx beams of the workload (for ncu captures)."""
     import torch
     from cos_gb300 import _lib, capon, synth
     x = synth.config1(seed=1, Nx=args.profile_nx)["x"]
@@ -408,7 +486,7 @@ def run_profile_case(args) -> None:
                           P=torch.empty((args.profile_nx, NY - 2 * K), dtype=torch.float32, device="cuda"))
     ctx = capon.Context()
     for _ in range(args.warmup + args.steps):
-        capon.capon_frames([f], ctx, capon.opts(form=_lib.FORM_FUSED))
+        capon.capon_frames([f], ctx, capon.opts(form=args.profile_form))
     torch.cuda.synchronize()
     print(json.dumps({"profile_case": {"Nx": args.profile_nx, "launches": args.warmup + args.steps}}))
 
@@ -420,6 +498,8 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-precision", action="store_true", help="skip the precision-stress study")
+    ap.add_argument("--profile-form", type=int, default=0, help="form of the profiling case (COS_CAPON_FORM_*)")
     ap.add_argument("--profile-nx", type=int, default=0,
                     help="profiling case: only the fused kernel, warmup+steps launches on Nx beams of the workload")
     args = ap.parse_args()

@@ -36,7 +36,8 @@
 namespace cgb {
 namespace tc {
 
-static constexpr int kThreads = 128;   // four warps: one per 32-lane TMEM quadrant
+static constexpr int kThreads = 256;   // eight warps, two per 32-lane TMEM quadrant
+static constexpr int kMaxTracePartials = 256;  // P * nseg <= kThreads
 static constexpr int kTmemCols = 512;  // the whole TMEM of the SM (one CTA per SM)
 static constexpr int kMinSmem = 116 * 1024;  // forces one resident CTA per SM
 
@@ -54,6 +55,7 @@ struct Geom {
     int slotBytes;  // all copies of A and B of one slot
     int opBytes;    // S slots
     int bs;         // band row stride in floats (even, L+2)
+    int nseg;       // segments per diagonal in the smoothing (P*L*nseg <= threads)
     int smem;
     uint32_t idesc;
 };
@@ -175,6 +177,8 @@ COS_DEV void split(float v, uint32_t &hi, uint32_t &lo)
 COS_DEV int core_off(int r, int kc, int sbo) { return (r >> 3) * sbo + kc * 128 + (r & 7) * 16; }
 
 // ---- the kernel -------------------------------------------------------------------------
+// Eight warps: warps w and w+4 share TMEM lane quadrant w%4 and split its
+// columns on readout.
 template <int SPLIT>
 __global__ void __launch_bounds__(kThreads, 1) tc_cov_kernel(const __grid_constant__ Params prm)
 {
@@ -188,7 +192,8 @@ __global__ void __launch_bounds__(kThreads, 1) tc_cov_kernel(const __grid_consta
     unsigned char *ops = smem;                                       // S slots of operands
     float *bandRe = (float *)(smem + g.opBytes);                     // [128][bs]
     float *bandIm = bandRe + 128 * g.bs;                             // [128][bs]
-    uint64_t *bar = (uint64_t *)(bandIm + 128 * g.bs);
+    float *trp = bandIm + 128 * g.bs;                                // [P][nseg] trace partials
+    uint64_t *bar = (uint64_t *)(trp + kMaxTracePartials);
     uint32_t *tmem_slot = (uint32_t *)(bar + 1);
     int *flag = (int *)(tmem_slot + 1);
     float2 *Rst = (float2 *)ops;                                      // staged R of one slot
@@ -199,6 +204,9 @@ __global__ void __launch_bounds__(kThreads, 1) tc_cov_kernel(const __grid_consta
     const int kchunks = g.Ktot / g.E;
     const int sbo = kchunks * 128;
     const int rows_ab = 128 + g.N;
+    // this thread's operand rows (fixed for the kernel): A rows, then B rows
+    // diagonal segments of the smoothing: P*L diagonals x nseg pieces
+    const int nseg = g.nseg, seglen = (L + nseg - 1) / nseg;
 
     if (warp == 0) tmem_alloc(tmem_slot, kTmemCols);
     if (tid == 0) {
@@ -213,54 +221,66 @@ __global__ void __launch_bounds__(kThreads, 1) tc_cov_kernel(const __grid_consta
 
     for (long long u = blockIdx.x; u < units; u += gridDim.x) {
         const long long pix0 = u * per_pass;
-        // 1. operands: A and B of every slot, hi (and lo) copies
-        const int total = g.S * kchunks * rows_ab;
-        for (int idx = tid; idx < total; idx += kThreads) {
-            const int row = idx % rows_ab;
-            const int kc = (idx / rows_ab) % kchunks;
-            const int s = idx / (rows_ab * kchunks);
-            const bool isA = row < 128;
-            int p = 0, ch = 0, part = 0;   // part: 0 A, 1 B re columns, 2 B im columns, 3 zero
-            if (isA) {
-                p = row / M;
-                ch = row % M;
-                part = p < g.P ? 0 : 3;
-            } else {
-                const int n = row - 128;
-                part = n < M ? 1 : (n < 2 * M ? 2 : 3);
-                ch = n < M ? n : n - M;
-            }
-            uint32_t hi[8], lo[8];
+        // 1. operands: A and B of every slot, hi (and lo) copies.  For a fixed
+        // (slot, K chunk) the (pixel, window row) of each element pair is the
+        // same for every operand row, so it is resolved once per chunk.
+        for (int sk = 0; sk < g.S * kchunks; ++sk) {
+            const int s = sk / kchunks, kc = sk % kchunks;
+            const float2 *rowp[4];
+            int pkv[4];
 #pragma unroll
-            for (int e = 0; e < 8; e += 2) {
-                float2 v = make_float2(0.f, 0.f);
-                const int k = kc * g.E + e;   // even: the real part of (p', t)
-                if (e < g.E && part != 3) {
+            for (int e = 0; e < 4; ++e) {
+                rowp[e] = nullptr;
+                pkv[e] = -1;
+                const int k = kc * g.E + 2 * e;   // even: the real part of (p', t)
+                if (2 * e < g.E) {
                     const int pk = k / twoT, t = (k % twoT) >> 1;
                     const long long pix = pix0 + (long long)s * g.P + pk;
-                    if (pk < g.P && pix < npix && (part != 0 || pk == p)) {
+                    if (pk < g.P && pix < npix) {
                         const int bx = (int)(pix / f.Npy), py = (int)(pix % f.Npy);
-                        v = __ldg(f.x + ((size_t)bx * f.Ny + py + t) * M + ch);
-                        if (part == 2) v = make_float2(-v.y, v.x);
+                        rowp[e] = f.x + ((size_t)bx * f.Ny + py + t) * M;
+                        pkv[e] = pk;
                     }
                 }
-                split<SPLIT>(v.x, hi[e], lo[e]);
-                split<SPLIT>(v.y, hi[e + 1], lo[e + 1]);
-            }
-            uint4 h4, l4;
-            if (BF16) {
-                h4 = make_uint4(hi[0] | (hi[1] << 16), hi[2] | (hi[3] << 16), hi[4] | (hi[5] << 16),
-                                hi[6] | (hi[7] << 16));
-                l4 = make_uint4(lo[0] | (lo[1] << 16), lo[2] | (lo[3] << 16), lo[4] | (lo[5] << 16),
-                                lo[6] | (lo[7] << 16));
-            } else {
-                h4 = make_uint4(hi[0], hi[1], hi[2], hi[3]);
-                l4 = make_uint4(lo[0], lo[1], lo[2], lo[3]);
             }
             unsigned char *slot = ops + (size_t)s * g.slotBytes;
-            const int off = isA ? core_off(row, kc, sbo) : g.aBytes + core_off(row - 128, kc, sbo);
-            *(uint4 *)(slot + off) = h4;
-            if (NT == 3) *(uint4 *)(slot + g.aBytes + g.bBytes + off) = l4;
+            for (int row = tid; row < rows_ab; row += kThreads) {
+                const bool isA = row < 128;
+                int p = 0, ch = 0, part = 0;   // part: 0 A, 1 B re columns, 2 B im columns, 3 zero
+                if (isA) {
+                    p = row / M;
+                    ch = row - p * M;
+                    part = p < g.P ? 0 : 3;
+                } else {
+                    const int n = row - 128;
+                    part = n < M ? 1 : (n < 2 * M ? 2 : 3);
+                    ch = n < M ? n : n - M;
+                }
+                uint32_t hi[8], lo[8];
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    float2 v = make_float2(0.f, 0.f);
+                    if (rowp[e] && part != 3 && (part != 0 || pkv[e] == p)) {
+                        v = __ldg(rowp[e] + ch);
+                        if (part == 2) v = make_float2(-v.y, v.x);
+                    }
+                    split<SPLIT>(v.x, hi[2 * e], lo[2 * e]);
+                    split<SPLIT>(v.y, hi[2 * e + 1], lo[2 * e + 1]);
+                }
+                uint4 h4, l4;
+                if (BF16) {
+                    h4 = make_uint4(hi[0] | (hi[1] << 16), hi[2] | (hi[3] << 16), hi[4] | (hi[5] << 16),
+                                    hi[6] | (hi[7] << 16));
+                    l4 = make_uint4(lo[0] | (lo[1] << 16), lo[2] | (lo[3] << 16), lo[4] | (lo[5] << 16),
+                                    lo[6] | (lo[7] << 16));
+                } else {
+                    h4 = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+                    l4 = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+                }
+                const int off = isA ? core_off(row, kc, sbo) : g.aBytes + core_off(row - 128, kc, sbo);
+                *(uint4 *)(slot + off) = h4;
+                if (NT == 3) *(uint4 *)(slot + g.aBytes + g.bBytes + off) = l4;
+            }
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
@@ -304,12 +324,13 @@ __global__ void __launch_bounds__(kThreads, 1) tc_cov_kernel(const __grid_consta
         for (int s = 0; s < g.S; ++s) {
             const long long spix = pix0 + (long long)s * g.P;
             if (spix >= npix) break;
-            const int r = warp * 32 + lane;            // this thread's TMEM lane: row (p, m)
+            const int q4 = warp & 3;                   // TMEM lane quadrant
+            const int r = q4 * 32 + lane;              // this thread's TMEM lane: row (p, m)
             const int p = r / M, m = r % M;
             const bool rv = p < g.P;
-            for (int c0 = 0; c0 < 2 * M; c0 += 32) {
+            for (int c0 = 32 * (warp >> 2); c0 < 2 * M; c0 += 64) {
                 uint32_t v[32];
-                tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(s * g.N + c0), v);
+                tmem_ld32(tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)(s * g.N + c0), v);
 #pragma unroll
                 for (int q = 0; q < 32; ++q) {
                     const int col = c0 + q;
@@ -319,42 +340,45 @@ __global__ void __launch_bounds__(kThreads, 1) tc_cov_kernel(const __grid_consta
                 }
             }
             __syncthreads();
-            // one thread per (pixel, diagonal): sliding float-float window sums
+            // one thread per (pixel, diagonal, segment of the diagonal): sliding
+            // float-float window sums, each segment starting from a full sum
             const int np = (int)min((long long)g.P, npix - spix);
-            if (tid < np * L) {
-                const int pp = tid / L, dg = tid % L;
+            if (tid < np * L * nseg) {
+                const int sg = tid % nseg, dg = (tid / nseg) % L, pp = tid / (nseg * L);
+                const int j0 = sg * seglen, j1 = min(j0 + seglen, L - dg);
                 const float *gr = bandRe + (size_t)pp * M * g.bs + dg;
                 const float *gi = bandIm + (size_t)pp * M * g.bs + dg;
-                float2 h = make_float2(0.f, 0.f), l = make_float2(0.f, 0.f);
-                for (int i = 0; i < Ns; ++i) two_sum_acc(h, l, make_float2(gr[i * g.bs], gi[i * g.bs]));
                 float2 *Rp = Rst + (size_t)pp * L * L;
-                float trh = 0.f, trl = 0.f;
-                for (int j = 0; j + dg < L; ++j) {
-                    if (j > 0) {
-                        two_sum_acc(h, l, make_float2(gr[(j + Ns - 1) * g.bs], gi[(j + Ns - 1) * g.bs]));
-                        two_sum_acc(h, l, make_float2(-gr[(j - 1) * g.bs], -gi[(j - 1) * g.bs]));
-                    }
-                    const float2 vv = fadd2(h, l);
-                    Rp[j + (j + dg) * L] = vv;
-                    if (dg) {
-                        Rp[(j + dg) + j * L] = cconj(vv);
-                    } else {
-                        const float t2 = trh + vv.x;
-                        trl += (trh - (t2 - (t2 - trh))) + (vv.x - (t2 - trh));
-                        trh = t2;
+                float tr = 0.f;
+                if (j0 < j1) {
+                    float2 h = make_float2(0.f, 0.f), l = make_float2(0.f, 0.f);
+                    for (int i = j0; i < j0 + Ns; ++i) two_sum_acc(h, l, make_float2(gr[i * g.bs], gi[i * g.bs]));
+                    for (int j = j0; j < j1; ++j) {
+                        if (j > j0) {
+                            two_sum_acc(h, l, make_float2(gr[(j + Ns - 1) * g.bs], gi[(j + Ns - 1) * g.bs]));
+                            two_sum_acc(h, l, make_float2(-gr[(j - 1) * g.bs], -gi[(j - 1) * g.bs]));
+                        }
+                        const float2 vv = fadd2(h, l);
+                        Rp[j + (j + dg) * L] = vv;
+                        if (dg)
+                            Rp[(j + dg) + j * L] = cconj(vv);
+                        else
+                            tr += vv.x;
                     }
                 }
-                if (dg == 0) {
-                    const float tr = trh + trl;
-                    prm.dl[spix + pp] = f.loading == COS_CAPON_LOAD_ABSOLUTE ? f.d * (float)(Ns * T)
-                                                                             : f.d * tr / (float)L;
-                }
+                if (dg == 0) trp[pp * nseg + sg] = tr;
             }
             __syncthreads();
+            if (tid < np) {
+                float tr = 0.f;
+                for (int sg = 0; sg < nseg; ++sg) tr += trp[tid * nseg + sg];
+                prm.dl[spix + tid] = f.loading == COS_CAPON_LOAD_ABSOLUTE ? f.d * (float)(Ns * T) : f.d * tr / (float)L;
+            }
             // the slot's R block is contiguous in HBM
             const int n2 = np * L * L;
             float2 *dst = prm.Rw + (size_t)spix * L * L;
             for (int i = tid; i < n2; i += kThreads) dst[i] = Rst[i];
+            __syncthreads();
         }
         tc_fence_before();
         __syncthreads();
@@ -387,8 +411,10 @@ static bool tc_geometry(const FrameDev &f, int split, Geom &g)
     g.bBytes = g.N * g.Ktot * g.esize;
     g.slotBytes = g.copies * (g.aBytes + g.bBytes);
     g.bs = L + 2;   // odd float offset between rows' writes of one band column
-    const int bandBytes = 2 * 128 * g.bs * (int)sizeof(float);
+    const int bandBytes = 2 * 128 * g.bs * (int)sizeof(float) + kMaxTracePartials * (int)sizeof(float);
     const int tail = 64;
+    g.nseg = kThreads / (g.P * L);
+    if (g.nseg > L) g.nseg = L;
     const int rstBytes = g.P * L * L * (int)sizeof(float2);
     g.S = kTmemCols / g.N;
     if (g.S > 4) g.S = 4;
