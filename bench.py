@@ -475,20 +475,90 @@ def precision_study(ctx, stream) -> dict:
     return out
 
 
+RTC_STAGES = ["memcpy_x_h2d", "sliding_beamspace", "build_R", "memcpy_R_d2h", "init_a", "beamspace_part1",
+              "solve", "beamspace_part2", "weights_output", "memcpy_wz_d2h"]
+
+
+def run_rtc(args) -> None:
+    """The reference's own RealTimeCapon GPU library (built from its sources by
+    oracle/build_rtc.py) on the same workload: its per-stage wall times (the
+    library's timer file), the kernel-stage sum, and its P error vs the oracle."""
+    import ctypes
+    import tempfile
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import build_rtc  # noqa: E402
+    import oracle  # noqa: E402
+    from cos_gb300 import synth
+    libpath = build_rtc.build()
+    if not libpath:
+        print(json.dumps({"impl": "reference-gpu-library", "unavailable": "reference sources not staged"}))
+        return
+    rtc = ctypes.CDLL(libpath)
+    vp, fl, i = ctypes.c_void_p, ctypes.c_float, ctypes.c_int
+    rtc.rtc_get_capon.argtypes = [vp, vp, vp, vp, fl, i, i, i, i, i, i]
+    x = synth.config1(seed=1)["x"]
+    npy = NY - 2 * K
+    z = np.zeros((NX, npy), np.complex64)
+    w = np.zeros((NX, npy, L), np.complex64)
+    R = np.zeros((NX, npy, L, L), np.complex64)   # the library copies R back (COPY_R_DEVICE_HOST)
+    cwd = os.getcwd()
+    tmp = tempfile.mkdtemp(prefix="rtc_")
+    os.chdir(tmp)
+    try:
+        calls = []
+        for it in range(1 + max(1, args.steps)):
+            t0 = time.perf_counter()
+            e = rtc.rtc_get_capon(z.ctypes.data, w.ctypes.data, R.ctypes.data, x.ctypes.data, D, L, K, M, NX, NY, 0)
+            calls.append((time.perf_counter() - t0) * 1e3)
+            if e:
+                print(json.dumps({"impl": "reference-gpu-library", "error": int(e)}))
+                return
+        rows = [[float(v) for v in ln.split()] for ln in open("timer_values.txt") if ln.strip()]
+    finally:
+        os.chdir(cwd)
+    rows = rows[1:]   # the first call allocates
+    med = {n: statistics.median(r[k] for r in rows) for k, n in enumerate(RTC_STAGES)}
+    kern = med["build_R"] + med["init_a"] + med["solve"] + med["weights_output"]
+    beams = [0, 128, 255]
+    ref = oracle.capon(np.ascontiguousarray(x[beams]), D, L, K, want_w=False, nthreads=3)
+    # the library returns z and w; its power is 1/Re(sum Ria) = w^H R w with w = Ria/sum(Ria)
+    Rb = R[beams].astype(np.complex128) / (NS * T)    # column-major, loaded, unnormalised -> normalised
+    wb = w[beams].astype(np.complex128)
+    P = np.real(np.einsum("bpi,bpji,bpj->bp", wb.conj(), Rb, wb))
+    relP = np.abs(P - ref["P"]) / ref["P"]
+    relz = np.abs(z[beams] - ref["z"]) / np.sqrt(ref["P"])
+    print(json.dumps({
+        "impl": "reference-gpu-library", "workload": CONFIG["workload"], "pixels": NPIX,
+        "stages_ms_median": med, "kernel_stages_ms": kern, "pixels_per_s_kernel_stages": NPIX / (kern * 1e-3),
+        "call_ms_median": statistics.median(calls[1:]), "calls": len(calls) - 1,
+        "P_rel_err_max": float(relP.max()), "z_err_max_rel_sqrtP": float(relz.max()),
+        "note": "RealTimeCapon built from its own sources for sm_103a; stage times are the library's own "
+                "host wall-clock timers around synchronised stages (Capon.cpp:171-459)"}))
+
+
 def run_profile_case(args) -> None:
-    """One form (default: fused) alone on Nx=profile_nx beams of the workload (for ncu captures)."""
+    """One form (default: fused) alone on the first Nx=profile_nx beams of a
+    workload (config1, config2 = its four frames, config3), for ncu captures."""
     import torch
-    from cos_gb300 import _lib, capon, synth
-    x = synth.config1(seed=1, Nx=args.profile_nx)["x"]
-    xt = torch.from_numpy(x).cuda()
-    f = capon.DeviceFrame(x=xt, L=L, K=K, d=D,
-                          z=torch.empty((args.profile_nx, NY - 2 * K), dtype=torch.complex64, device="cuda"),
-                          P=torch.empty((args.profile_nx, NY - 2 * K), dtype=torch.float32, device="cuda"))
+    from cos_gb300 import capon, synth
+    wl = args.profile_workload
+    if wl == "config2":
+        cfgs = synth.config2(seed=2, Nx=args.profile_nx)
+    elif wl == "config3":
+        cfgs = [synth.config3(seed=3, Nx=args.profile_nx)]
+    else:
+        cfgs = [synth.config1(seed=1, Nx=args.profile_nx)]
+    frames = []
+    for c in cfgs:
+        Nx, Ny, _ = c["x"].shape
+        frames.append(capon.DeviceFrame(x=torch.from_numpy(c["x"]).cuda(), L=c["L"], K=c["K"], d=c["d"],
+                                        Nb=c["Nb"],
+                                        P=torch.empty((Nx, Ny - 2 * c["K"]), dtype=torch.float32, device="cuda")))
     ctx = capon.Context()
     for _ in range(args.warmup + args.steps):
-        capon.capon_frames([f], ctx, capon.opts(form=args.profile_form))
+        capon.capon_frames(frames, ctx, capon.opts(form=args.profile_form))
     torch.cuda.synchronize()
-    print(json.dumps({"profile_case": {"Nx": args.profile_nx, "launches": args.warmup + args.steps}}))
+    print(json.dumps({"profile_case": {"workload": wl, "Nx": args.profile_nx, "launches": args.warmup + args.steps}}))
 
 
 def main() -> None:
@@ -499,11 +569,16 @@ def main() -> None:
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-precision", action="store_true", help="skip the precision-stress study")
+    ap.add_argument("--rtc", action="store_true",
+                    help="time the reference's RealTimeCapon GPU library (oracle/build_rtc.py) on the workload")
     ap.add_argument("--profile-form", type=int, default=0, help="form of the profiling case (COS_CAPON_FORM_*)")
+    ap.add_argument("--profile-workload", default="config1", choices=["config1", "config2", "config3"])
     ap.add_argument("--profile-nx", type=int, default=0,
                     help="profiling case: only the fused kernel, warmup+steps launches on Nx beams of the workload")
     args = ap.parse_args()
-    if args.profile_nx:
+    if args.rtc:
+        run_rtc(args)
+    elif args.profile_nx:
         run_profile_case(args)
     elif args.impl == "reference":
         run_reference(args)

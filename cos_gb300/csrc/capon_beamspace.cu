@@ -21,6 +21,8 @@
 
 namespace cgb {
 
+int launch_beamspace_warp(const FrameDev &f, float2 *R_out, cudaStream_t s);
+
 static constexpr int kBsWarps = 4;
 
 struct BsSmem {
@@ -244,7 +246,345 @@ beamspace_kernel(FrameDev f, float2 *__restrict__ Rbs)
     }
 }
 
+// ---------------------------------------------------------------------------
+// Range-tile kernel for small beam counts (Nb <= 5).  A range row's subarray
+// DFTs are shared by the 2K+1 pixels whose window contains the row, so they
+// are computed once per row:
+//   phase A  one half-warp per row: lane q slides the DFT over subarrays
+//            [q c, q c + c) (a direct DFT at the chunk start, then the
+//            recurrence), sums its Y Y^H products in FP32 and reduces across
+//            the half-warp in float-float -> Q_row (Nb x Nb upper, hi + lo),
+//            the row's snapshot energy and beam sums sum_s Y_s;
+//   phase B  one thread per pixel: R_bs = sum of the window's Q rows
+//            (float-float), loading, FP32 Cholesky, one FP64-residual
+//            refinement step, P and z (g_bs = B g = the centre row's beam sums / Ns);
+//   phase C  (w requested) w = B^H x_bs / a_bs^H x_bs, one thread per output.
+static constexpr int kTileThreads = 256;
+
+template <int NB>
+struct BsTile {
+    static constexpr int NQ = NB * (NB + 1) / 2;
+};
+
+struct BsTileSmem {
+    int rows, tile;
+    size_t off_x, off_q, off_e, off_g, off_b, off_xs, total;
+    __host__ __device__ BsTileSmem(int tile_, int K, int M, int L, int NB)
+    {
+        tile = tile_;
+        rows = tile + 2 * K;
+        const int NQ = NB * (NB + 1) / 2;
+        off_x = 0;                                                          // rows x M
+        off_q = off_x + (((size_t)rows * M * sizeof(float2) + 15) & ~(size_t)15);   // rows x 2NQ (hi, lo)
+        off_e = off_q + (size_t)rows * 2 * NQ * sizeof(float2);             // rows: energy
+        off_g = off_e + (((size_t)rows * sizeof(float) + 15) & ~(size_t)15); // rows x NB: beam sums
+        off_b = off_g + (size_t)rows * NB * sizeof(float2);                 // Butler NB x L, rot NB, a_bs NB
+        off_xs = off_b + (size_t)(NB * L + 2 * NB) * sizeof(float2);        // tile x (NB + 1): x_bs, 1/sum
+        total = off_xs + (size_t)tile * (NB + 1) * sizeof(float2);
+    }
+};
+
+template <int NB>
+__global__ void __launch_bounds__(kTileThreads)
+beamspace_tile_kernel(FrameDev f, float2 *__restrict__ Rbs, int tile)
+{
+    constexpr int NQ = BsTile<NB>::NQ;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    const int M = f.M, L = f.L, K = f.K, T = 2 * K + 1, Ns = M - L + 1;
+    const BsTileSmem S(tile, K, M, L, NB);
+    float2 *xs = (float2 *)(smraw + S.off_x);
+    float2 *Qs = (float2 *)(smraw + S.off_q);
+    float *Es = (float *)(smraw + S.off_e);
+    float2 *Gs = (float2 *)(smraw + S.off_g);
+    float2 *Bt = (float2 *)(smraw + S.off_b);
+    float2 *rot = Bt + NB * L;
+    float2 *ab = rot + NB;
+    float2 *Xb = (float2 *)(smraw + S.off_xs);
+    const int tid = threadIdx.x;
+    const float isl = 1.0f / sqrtf((float)L);
+
+    const int tiles_per_beam = (f.Npy + tile - 1) / tile;
+    const int bx = blockIdx.x / tiles_per_beam;
+    const int p0 = (blockIdx.x % tiles_per_beam) * tile;
+    const int np = min(tile, f.Npy - p0);
+    const int rows = np + 2 * K;
+
+    // Butler table and the a_bs = B 1 of this launch
+    for (int i = tid; i < NB * L; i += kTileThreads) {
+        const int bb = i / L, l = i % L;
+        float sn, cs;
+        sincospif(2.0f * (float)((butler_bin(bb, NB, L) * l) % L) / (float)L, &sn, &cs);
+        Bt[i] = make_float2(cs * isl, -sn * isl);
+    }
+    if (tid < NB) {
+        float sn, cs;
+        sincospif(2.0f * (float)butler_bin(tid, NB, L) / (float)L, &sn, &cs);
+        rot[tid] = make_float2(cs, sn);
+    }
+    // stage the tile's rows (one contiguous run of the beam)
+    const float2 *src = f.x + ((size_t)bx * f.Ny + p0) * M;
+    for (int i = tid; i < rows * M; i += kTileThreads) xs[i] = src[i];
+    __syncthreads();
+    if (tid < NB) {
+        float2 acc = make_float2(0.f, 0.f);
+        for (int l = 0; l < L; ++l) acc = cadd(acc, Bt[tid * L + l]);
+        ab[tid] = acc;
+    }
+
+    // ---- phase A: per-row terms, one half-warp per row
+    {
+        const int half = (tid >> 4) & 1, q = tid & 15, warp = tid >> 5;
+        const int c = (Ns + 15) / 16;
+        const int s0 = q * c, s1 = min(Ns, s0 + c);
+        for (int base = 2 * warp; base < rows; base += kTileThreads / 16) {
+            const int r = base + half;
+            float2 P[NQ], Yg[NB];
+            float en = 0.f;
+#pragma unroll
+            for (int e = 0; e < NQ; ++e) P[e] = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int b = 0; b < NB; ++b) Yg[b] = make_float2(0.f, 0.f);
+            if (r < rows && s0 < s1) {
+                const float2 *xr = xs + (size_t)r * M;
+                float2 Y[NB];
+#pragma unroll
+                for (int b = 0; b < NB; ++b) Y[b] = make_float2(0.f, 0.f);
+                float e = 0.f;
+                for (int l = 0; l < L; ++l) {
+                    const float2 v = xr[s0 + l];
+                    e += cabs2(v);
+#pragma unroll
+                    for (int b = 0; b < NB; ++b) Y[b] = cadd(Y[b], cmul(Bt[b * L + l], v));
+                }
+                for (int s = s0; s < s1; ++s) {
+                    if (s > s0) {
+                        const float2 dx = cscale(csub(xr[s - 1 + L], xr[s - 1]), isl);
+                        e += cabs2(xr[s - 1 + L]) - cabs2(xr[s - 1]);
+#pragma unroll
+                        for (int b = 0; b < NB; ++b) Y[b] = cmul(rot[b], cadd(Y[b], dx));
+                    }
+                    en += e;
+#pragma unroll
+                    for (int i = 0; i < NB; ++i) {
+                        Yg[i] = cadd(Yg[i], Y[i]);
+#pragma unroll
+                        for (int j = i; j < NB; ++j) {
+                            const int k = i * NB - i * (i - 1) / 2 + (j - i);
+                            P[k] = cadd(P[k], cmulc(Y[i], Y[j]));
+                        }
+                    }
+                }
+            }
+            // float-float reduction over the half-warp
+            float2 lo[NQ];
+#pragma unroll
+            for (int e = 0; e < NQ; ++e) lo[e] = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int o = 8; o; o >>= 1) {
+#pragma unroll
+                for (int e = 0; e < NQ; ++e) {
+                    const float2 oh = shfl2_xor(P[e], o, 16), ol = shfl2_xor(lo[e], o, 16);
+                    two_sum_acc(P[e], lo[e], oh);
+                    lo[e] = fadd2(lo[e], ol);
+                }
+#pragma unroll
+                for (int b = 0; b < NB; ++b) Yg[b] = cadd(Yg[b], shfl2_xor(Yg[b], o, 16));
+                en += __shfl_xor_sync(0xffffffffu, en, o, 16);
+            }
+            if (r < rows && q == 0) {
+#pragma unroll
+                for (int e = 0; e < NQ; ++e) {
+                    Qs[(size_t)r * 2 * NQ + e] = P[e];
+                    Qs[(size_t)r * 2 * NQ + NQ + e] = lo[e];
+                }
+                Es[r] = en;
+#pragma unroll
+                for (int b = 0; b < NB; ++b) Gs[(size_t)r * NB + b] = Yg[b];
+            }
+        }
+    }
+    __syncthreads();
+
+    // ---- phase B: one thread per pixel
+    for (int lp = tid; lp < np; lp += kTileThreads) {
+        float2 Rh[NQ], Rl[NQ];
+        float tr = 0.f;
+#pragma unroll
+        for (int e = 0; e < NQ; ++e) {
+            Rh[e] = make_float2(0.f, 0.f);
+            Rl[e] = make_float2(0.f, 0.f);
+        }
+        for (int t = 0; t < T; ++t) {
+            const float2 *qr = Qs + (size_t)(lp + t) * 2 * NQ;
+#pragma unroll
+            for (int e = 0; e < NQ; ++e) {
+                two_sum_acc(Rh[e], Rl[e], qr[e]);
+                Rl[e] = fadd2(Rl[e], qr[NQ + e]);
+            }
+            tr += Es[lp + t];
+        }
+        // renormalise: (Rh, Rl) -> rounded value + remainder
+#pragma unroll
+        for (int e = 0; e < NQ; ++e) {
+            const float2 v = fadd2(Rh[e], Rl[e]);
+            Rl[e] = fsub2(Rl[e], fsub2(v, Rh[e]));
+            Rh[e] = v;
+        }
+        float dl;
+        if (f.loading == COS_CAPON_LOAD_ABSOLUTE) {
+            dl = f.d * (float)(Ns * T);
+        } else if (f.loading == COS_CAPON_LOAD_BEAMSPACE) {
+            float tb = 0.f;
+            int k = 0;
+#pragma unroll
+            for (int i = 0; i < NB; ++i) {
+                tb += Rh[k].x;
+                k += NB - i;
+            }
+            dl = f.d * tb / (float)NB;
+        } else {
+            dl = f.d * tr / (float)L;
+        }
+        const long long pix = (long long)bx * f.Npy + p0 + lp;
+        if (Rbs) {  // loaded, unnormalised, column-major
+            float2 *Rp = Rbs + (size_t)pix * NB * NB;
+            int k = 0;
+#pragma unroll
+            for (int i = 0; i < NB; ++i)
+#pragma unroll
+                for (int j = i; j < NB; ++j, ++k) {
+                    const float2 v = (i == j) ? make_float2(Rh[k].x + dl, 0.f) : Rh[k];
+                    Rp[i + j * NB] = v;
+                    if (i != j) Rp[j + i * NB] = cconj(v);
+                }
+        }
+        // FP32 Cholesky of Rh + dl I (upper, packed rows)
+        float2 U[NQ];
+        {
+            int k = 0;
+#pragma unroll
+            for (int i = 0; i < NB; ++i)
+#pragma unroll
+                for (int j = i; j < NB; ++j, ++k) U[k] = (i == j) ? make_float2(Rh[k].x + dl, 0.f) : Rh[k];
+        }
+        auto idx = [](int i, int j) { return i * NB - i * (i - 1) / 2 + (j - i); };   // i <= j
+#pragma unroll
+        for (int i = 0; i < NB; ++i) {
+            float dv = U[idx(i, i)].x;
+#pragma unroll
+            for (int k = 0; k < i; ++k) dv -= cabs2(U[idx(k, i)]);
+            const float u = sqrtf(dv), iu = 1.0f / u;
+            U[idx(i, i)] = make_float2(u, 0.f);
+#pragma unroll
+            for (int j = i + 1; j < NB; ++j) {
+                float2 v = U[idx(i, j)];
+#pragma unroll
+                for (int k = 0; k < i; ++k) v = csub(v, cconjmul(U[idx(k, i)], U[idx(k, j)]));
+                U[idx(i, j)] = cscale(v, iu);
+            }
+        }
+        auto solve = [&](float2 (&v)[NB]) {
+#pragma unroll
+            for (int i = 0; i < NB; ++i) {
+#pragma unroll
+                for (int k = 0; k < i; ++k) v[i] = csub(v[i], cconjmul(U[idx(k, i)], v[k]));
+                v[i] = cscale(v[i], 1.0f / U[idx(i, i)].x);
+            }
+#pragma unroll
+            for (int i = NB - 1; i >= 0; --i) {
+#pragma unroll
+                for (int k = i + 1; k < NB; ++k) v[i] = csub(v[i], cmul(U[idx(i, k)], v[k]));
+                v[i] = cscale(v[i], 1.0f / U[idx(i, i)].x);
+            }
+        };
+        float2 xb[NB], r[NB];
+#pragma unroll
+        for (int i = 0; i < NB; ++i) xb[i] = ab[i];
+        solve(xb);
+        // FP64 residual against the float-float matrix, one correction
+#pragma unroll
+        for (int i = 0; i < NB; ++i) {
+            double rr = (double)ab[i].x, ri = (double)ab[i].y;
+#pragma unroll
+            for (int j = 0; j < NB; ++j) {
+                double ar, ai;
+                if (i <= j) {
+                    const int k = idx(i, j);
+                    ar = (double)Rh[k].x + (double)Rl[k].x + (i == j ? (double)dl : 0.0);
+                    ai = (i == j) ? 0.0 : (double)Rh[k].y + (double)Rl[k].y;
+                } else {
+                    const int k = idx(j, i);
+                    ar = (double)Rh[k].x + (double)Rl[k].x;
+                    ai = -((double)Rh[k].y + (double)Rl[k].y);
+                }
+                rr -= ar * (double)xb[j].x - ai * (double)xb[j].y;
+                ri -= ar * (double)xb[j].y + ai * (double)xb[j].x;
+            }
+            r[i] = make_float2((float)rr, (float)ri);
+        }
+        solve(r);
+        float2 aRa = make_float2(0.f, 0.f), zn = make_float2(0.f, 0.f);
+        const float2 *gc = Gs + (size_t)(lp + K) * NB;
+#pragma unroll
+        for (int i = 0; i < NB; ++i) {
+            xb[i] = cadd(xb[i], r[i]);
+            aRa = cadd(aRa, cconjmul(ab[i], xb[i]));
+            zn = cadd(zn, cconjmul(xb[i], gc[i]));
+        }
+        // sum(Ria) = a_bs^H x_bs; z = conj(x_bs)^T g_bs / conj(sum), g_bs = beam sums / Ns
+        const float den = cabs2(aRa);
+        const float2 isum = make_float2(aRa.x / den, -aRa.y / den);      // 1 / sum
+        const float2 zz = cscale(cmul(zn, cconj(isum)), 1.0f / (float)Ns);
+        if (f.z) f.z[pix] = zz;
+        if (f.P) f.P[pix] = 1.0f / ((float)Ns * (float)T * aRa.x);
+#pragma unroll
+        for (int i = 0; i < NB; ++i) Xb[(size_t)lp * (NB + 1) + i] = xb[i];
+        Xb[(size_t)lp * (NB + 1) + NB] = isum;
+    }
+    if (f.w) {
+        __syncthreads();
+        // ---- phase C: w = B^H x_bs / sum, one thread per (pixel, element)
+        for (int i = tid; i < np * L; i += kTileThreads) {
+            const int lp = i / L, l = i % L;
+            const float2 *xv = Xb + (size_t)lp * (NB + 1);
+            float2 ria = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int b = 0; b < NB; ++b) ria = cadd(ria, cconjmul(Bt[b * L + l], xv[b]));
+            f.w[((size_t)bx * f.Npy + p0) * L + i] = cmul(ria, xv[NB]);
+        }
+    }
+}
+
+template <int NB>
+static int launch_tile(const FrameDev &f, float2 *R_out, cudaStream_t s)
+{
+    int tile = 64;
+    while (tile > 8 && BsTileSmem(tile, f.K, f.M, f.L, NB).total > 227 * 1024) tile /= 2;
+    const BsTileSmem S(tile, f.K, f.M, f.L, NB);
+    if (S.total > 227 * 1024) return cudaErrorNotSupported;
+    cudaError_t e = cudaFuncSetAttribute(beamspace_tile_kernel<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)S.total);
+    if (e != cudaSuccess) return e;
+    const long long blocks = (long long)f.Nx * ((f.Npy + tile - 1) / tile);
+    beamspace_tile_kernel<NB><<<(unsigned)blocks, kTileThreads, S.total, s>>>(f, R_out, tile);
+    return cudaGetLastError();
+}
+
 int launch_beamspace(const FrameDev &f, float2 *R_out, cudaStream_t s)
+{
+    switch (f.Nb) {
+    case 1: return launch_tile<1>(f, R_out, s);
+    case 2: return launch_tile<2>(f, R_out, s);
+    case 3: return launch_tile<3>(f, R_out, s);
+    case 4: return launch_tile<4>(f, R_out, s);
+    case 5: return launch_tile<5>(f, R_out, s);
+    default: break;
+    }
+    return launch_beamspace_warp(f, R_out, s);
+}
+
+// one warp per pixel: any Nb <= L
+int launch_beamspace_warp(const FrameDev &f, float2 *R_out, cudaStream_t s)
 {
     if (f.L > 64) return cudaErrorNotSupported;
     const BsSmem S(f.M, f.L, f.K, f.Nb);
