@@ -119,8 +119,17 @@ precise_build_r_kernel(FrameDev f, float2 *__restrict__ Rhi, float2 *__restrict_
     if (lane == 0) dlo[pix] = f.loading == COS_CAPON_LOAD_ABSOLUTE ? f.d * (float)(Ns * T) : f.d * tr / (float)L;
 }
 
-// One warp per pixel: FP32 Cholesky of R_hi + dl I in shared memory (row-major
-// upper factor), x0 = R^-1 a; with REFINE one FP64-residual correction step.
+// One warp per pixel: FP32 Cholesky of R_hi + dl I in shared memory, x0 =
+// R^-1 a; with REFINE one FP64-residual correction step.
+//
+// The upper triangle is stored packed by rows (row k at k*L - k(k-1)/2, L(L+1)/2
+// entries: 16.6 KB at L = 64, so several warps share an SM).  Step i of the
+// right-looking factorisation updates the pairs (k, j), i < k <= j < L; a
+// CTA-wide table lists all pairs by decreasing k, so the trailing set of step i
+// is the table's prefix of length n(n+1)/2, n = L-1-i, and the 32 lanes take
+// equal, independent shares of it.
+COS_DEV int prow(int k, int L) { return k * L - (k * (k - 1)) / 2; }
+
 template <bool REFINE>
 __global__ void __launch_bounds__(32 * kPrecWarps)
 precise_solve_kernel(int L, long long batch, const float2 *__restrict__ Rhi, const float2 *__restrict__ Rlo,
@@ -128,51 +137,68 @@ precise_solve_kernel(int L, long long batch, const float2 *__restrict__ Rhi, con
 {
     extern __shared__ float2 smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int NP = L * (L + 1) / 2;
+    uint16_t *pairs = (uint16_t *)(smem + (size_t)kPrecWarps * (NP + L));   // (k << 8) | j
+    // the pair table, shared by the CTA's warps
+    for (int e = threadIdx.x; e < NP; e += blockDim.x) {
+        // e-th pair by decreasing k: row k = L - n holds n pairs, at
+        // e in [n(n-1)/2, n(n+1)/2)
+        int n = (int)((sqrtf(8.f * (float)e + 1.f) - 1.f) * 0.5f);
+        while (n * (n + 1) / 2 <= e) ++n;
+        while (n > 1 && (n - 1) * n / 2 > e) --n;
+        const int k = L - n, j = k + (e - (n - 1) * n / 2);
+        pairs[e] = (uint16_t)((k << 8) | j);
+    }
+    __syncthreads();
     const long long sys = (long long)blockIdx.x * kPrecWarps + warp;
     if (sys >= batch) return;
-    const int ld = L + 1;
-    float2 *A = smem + (size_t)warp * (L * ld + 2 * L);
-    float2 *xb = A + (size_t)L * ld;   // x0 broadcast buffer
+    float2 *A = smem + (size_t)warp * (NP + L);
+    float2 *xb = A + NP;   // x0 broadcast buffer
     const float2 *Rh = Rhi + (size_t)sys * L * L, *Rl = Rlo ? Rlo + (size_t)sys * L * L : nullptr;
     const float dl = dlv[sys];
     for (int i = lane; i < L * L; i += 32) {
-        const int a = i % L, b = i / L;
-        float2 v = Rh[i];
-        if (a == b) v = make_float2(v.x + dl, 0.f);
-        A[a * ld + b] = v;
+        const int a = i % L, b = i / L;   // column-major source element (a, b)
+        if (a <= b) {
+            float2 v = Rh[i];
+            if (a == b) v = make_float2(v.x + dl, 0.f);
+            A[prow(a, L) + (b - a)] = v;
+        }
     }
     __syncwarp();
     bool bad = false;
     for (int i = 0; i < L; ++i) {
-        const float dv = A[i * ld + i].x;
+        float2 *Ai = A + prow(i, L);   // row i: Ai[j - i]
+        const float dv = Ai[0].x;
         bad |= !(dv > 0.f);
         const float inv = rsqrtf(dv);
         __syncwarp();
-        for (int j = i + 1 + lane; j < L; j += 32) A[i * ld + j] = cscale(A[i * ld + j], inv);
-        if (lane == 0) A[i * ld + i] = make_float2(dv * inv, 0.f);
+        for (int j = i + 1 + lane; j < L; j += 32) Ai[j - i] = cscale(Ai[j - i], inv);
+        if (lane == 0) Ai[0] = make_float2(dv * inv, 0.f);
         __syncwarp();
-        for (int j = i + 1 + lane; j < L; j += 32) {
-            const float2 uij = A[i * ld + j];
-            for (int k = i + 1; k <= j; ++k)
-                A[k * ld + j] = csub(A[k * ld + j], cconjmul(A[i * ld + k], uij));
+        const int n = L - 1 - i, cnt = n * (n + 1) / 2;
+        for (int e = lane; e < cnt; e += 32) {
+            const int kj = pairs[e], k = kj >> 8, j = kj & 255;
+            float2 &dst = A[prow(k, L) + (j - k)];
+            dst = csub(dst, cconjmul(Ai[k - i], Ai[j - i]));
         }
         __syncwarp();
     }
+    auto U = [&](int r, int c) { return A[prow(r, L) + (c - r)]; };   // r <= c
     // solve U^H U x = b for the lane-distributed right-hand side v (rows lane, lane+32)
     auto solve = [&](float2 &v0, float2 &v1) {
         for (int i = 0; i < L; ++i) {
             const float2 vi = shfl2(i < 32 ? v0 : v1, i & 31, 32);
-            const float2 yi = cscale(vi, 1.0f / A[i * ld + i].x);
-            if (lane > i && lane < L) v0 = csub(v0, cconjmul(A[i * ld + lane], yi));
-            if (lane + 32 > i && lane + 32 < L) v1 = csub(v1, cconjmul(A[i * ld + lane + 32], yi));
+            const float2 yi = cscale(vi, 1.0f / U(i, i).x);
+            if (lane > i && lane < L) v0 = csub(v0, cconjmul(U(i, lane), yi));
+            if (lane + 32 > i && lane + 32 < L) v1 = csub(v1, cconjmul(U(i, lane + 32), yi));
             if (lane == i) v0 = yi;
             if (lane + 32 == i) v1 = yi;
         }
         for (int i = L - 1; i >= 0; --i) {
             const float2 vi = shfl2(i < 32 ? v0 : v1, i & 31, 32);
-            const float2 xi = cscale(vi, 1.0f / A[i * ld + i].x);
-            if (lane < i) v0 = csub(v0, cmul(A[lane * ld + i], xi));
-            if (lane + 32 < i) v1 = csub(v1, cmul(A[(lane + 32) * ld + i], xi));
+            const float2 xi = cscale(vi, 1.0f / U(i, i).x);
+            if (lane < i) v0 = csub(v0, cmul(U(lane, i), xi));
+            if (lane + 32 < i) v1 = csub(v1, cmul(U(lane + 32, i), xi));
             if (lane == i) v0 = xi;
             if (lane + 32 == i) v1 = xi;
         }
@@ -245,7 +271,8 @@ int launch_precise_solve(const FrameDev &f, const float2 *Rhi, const float2 *Rlo
                          unsigned *status, bool refine, cudaStream_t s)
 {
     const long long npix = (long long)f.Nx * f.Npy;
-    const size_t sm2 = (size_t)kPrecWarps * (f.L * (f.L + 1) + 2 * f.L) * sizeof(float2);
+    const size_t sm2 = (size_t)kPrecWarps * (f.L * (f.L + 1) / 2 + f.L) * sizeof(float2) +
+                       (size_t)f.L * (f.L + 1) / 2 * sizeof(uint16_t);
     if (sm2 > 227 * 1024 || f.L > 64) return cudaErrorNotSupported;
     const long long blocks = (npix + kPrecWarps - 1) / kPrecWarps;
     cudaError_t e;
