@@ -32,7 +32,8 @@ EXPORTS = (
 
 
 class Opts(C.Structure):
-    _fields_ = [("form", C.c_int), ("loading", C.c_int), ("r_layout", C.c_int), ("refine", C.c_int)]
+    _fields_ = [("form", C.c_int), ("loading", C.c_int), ("r_layout", C.c_int), ("refine", C.c_int),
+                ("fb", C.c_int)]
 
 
 class Frame(C.Structure):

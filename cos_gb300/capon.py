@@ -34,8 +34,8 @@ def _ptr(a: np.ndarray) -> int:
 
 
 def opts(form: int = _lib.FORM_FUSED, loading: int = _lib.LOAD_ELEMENT, r_layout: int = _lib.R_REFERENCE,
-         refine: int = 0) -> Opts:
-    return Opts(form, loading, r_layout, refine)
+         refine: int = 0, fb: int = 0) -> Opts:
+    return Opts(form, loading, r_layout, refine, fb)
 
 
 class Context:
@@ -135,8 +135,10 @@ def getCaponCUDAPy(Xd, d, L, Navg, V, doFBAvg=False, verbose=False, want_R: bool
 def getCaponGPU(Xd, regCoef, L, Navg, V=None, doFBAvg=False, verbose=False, *, form=_lib.FORM_FUSED,
                 loading=_lib.LOAD_ELEMENT, want_w: bool = True):
     """getCaponCPy argument order on the GPU path: returns [z, P, w]
-    (complex64 z, float32 P, complex64 w or None).  Raises CaponError on a
-    nonzero status."""
+    (complex64 z, float32 P, complex64 w or None).  doFBAvg applies
+    forward-backward averaging (the reference CPU path accepts the flag and
+    ignores it, getCaponC.pyx:106; its definition is getCaponAllC.pyx:346-347).
+    Raises CaponError on a nonzero status."""
     Xd = np.ascontiguousarray(Xd, dtype=np.complex64)
     Nx, Ny, M = Xd.shape
     L, Navg = int(L), int(Navg)
@@ -145,7 +147,8 @@ def getCaponGPU(Xd, regCoef, L, Navg, V=None, doFBAvg=False, verbose=False, *, f
     P = np.zeros((Nx, Ny - 2 * Navg), np.float32)
     w = np.zeros((Nx, Ny - 2 * Navg, L), np.complex64) if want_w else None
     check(_module_ctx().getCaponEx(z, P, w, None, Xd, float(regCoef), L, Navg, M, Nx, Ny, Nb,
-                                   opts(form=form, loading=loading)), "cos_capon_get_capon_ex")
+                                   opts(form=form, loading=loading, fb=int(bool(doFBAvg)))),
+          "cos_capon_get_capon_ex")
     return [z, P, w]
 
 

@@ -64,7 +64,7 @@ struct cos_capon_ctx {
     cudaStream_t stream2 = nullptr;
 };
 
-static const cos_capon_opts kDefaultOpts = {COS_CAPON_FORM_FUSED, COS_CAPON_LOAD_ELEMENT, COS_CAPON_R_REFERENCE, 0};
+static const cos_capon_opts kDefaultOpts = {COS_CAPON_FORM_FUSED, COS_CAPON_LOAD_ELEMENT, COS_CAPON_R_REFERENCE, 0, 0};
 
 // Argument checks of Capon::getCapon (Capon.cpp:98-107) and BuildR::getR
 // (BuildR.cpp:37-48), plus this build's own limits.
@@ -110,6 +110,7 @@ static FrameDev make_frame(const cos_capon_frame &fr, const cos_capon_opts &o)
     f.loading = o.loading;
     f.r_layout = o.r_layout;
     f.refine = o.refine;
+    f.fb = o.fb ? 1 : 0;
     return f;
 }
 
@@ -128,7 +129,7 @@ static int candidates(int L, int K, const FusedCandidate **out)
 
 static bool use_fused(const FrameDev &f, const cos_capon_opts &o)
 {
-    if (o.form != COS_CAPON_FORM_FUSED || f.Nb != 0 || o.refine) return false;
+    if (o.form != COS_CAPON_FORM_FUSED || f.Nb != 0 || o.refine || o.fb) return false;
     const FusedCandidate *c = nullptr;
     const int n = candidates(f.L, f.K, &c);
     for (int i = 0; i < n; ++i)
@@ -214,11 +215,13 @@ static int run_plain(cos_capon_ctx *c, FrameDev f, cudaStream_t s)
     if ((e = c->Ria.ensure(npix * f.L * sizeof(float2)))) return e;
     float2 *Rw = (float2 *)c->Rwork.p, *Ria = (float2 *)c->Ria.p;
     if ((e = launch_plain_build_r(f, Rw, 1, s))) return e;
+    if (f.fb && (e = launch_fb_average(f, Rw, nullptr, s))) return e;
     if ((e = launch_plain_solve_hpd(f, Rw, Ria, c->d_status, s))) return e;
     if ((e = launch_plain_output(f, Ria, s))) return e;
     if (f.R) {
         // the requested R layout, written by a second covariance pass
         e = launch_plain_build_r(f, f.R, f.r_layout == COS_CAPON_R_REFERENCE ? 1 : 0, s);
+        if (!e && f.fb) e = launch_fb_average(f, f.R, nullptr, s);
     }
     return e;
 }
@@ -258,6 +261,7 @@ static int run_tc(cos_capon_ctx *c, FrameDev f, int split, bool refine, cudaStre
     float2 *Rw = (float2 *)c->Rwork.p;
     float *dl = (float *)c->dl.p;
     if ((e = launch_tc_covariance(f, split, Rw, dl, c->d_status, c->num_sms, s))) return e;
+    if (f.fb && (e = launch_fb_average(f, Rw, nullptr, s))) return e;
     if ((e = launch_precise_solve(f, Rw, nullptr, dl, (float2 *)c->Ria.p, c->d_status, refine, s))) return e;
     if (f.R) e = launch_format_r(f, Rw, nullptr, dl, f.R, s);
     return e;
@@ -269,6 +273,9 @@ static int run_frames(cos_capon_ctx *c, const FrameDev *fs, int n, const cos_cap
     if (is_tc_form(o.form))
         for (int k = 0; k < n; ++k)
             if (fs[k].Nb != 0 || !tc_supported(fs[k], o.form)) return COS_CAPON_ERR_NOT_SUPPORTED;
+    if (o.fb)
+        for (int k = 0; k < n; ++k)
+            if (fs[k].Nb > kBeamspaceTileMaxNb) return COS_CAPON_ERR_NOT_SUPPORTED;
     // batch consecutive fused frames with equal (L, K, M) into one launch
     int i = 0;
     while (i < n) {

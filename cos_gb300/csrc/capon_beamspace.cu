@@ -344,29 +344,34 @@ beamspace_tile_kernel(FrameDev f, float2 *__restrict__ Rbs, int tile)
             for (int e = 0; e < NQ; ++e) P[e] = make_float2(0.f, 0.f);
 #pragma unroll
             for (int b = 0; b < NB; ++b) Yg[b] = make_float2(0.f, 0.f);
-            if (r < rows && s0 < s1) {
+            // forward-backward averaging: the same products over the flipped,
+            // conjugated row x~[m] = conj(x[M-1-m]) (its covariance is
+            // J R^T J), halved at the end; energy and beam sums from x only
+            const int passes = f.fb ? 2 : 1;
+            for (int pass = 0; pass < passes && r < rows && s0 < s1; ++pass) {
                 const float2 *xr = xs + (size_t)r * M;
+                auto X = [&](int i) { return pass ? cconj(xr[M - 1 - i]) : xr[i]; };
                 float2 Y[NB];
 #pragma unroll
                 for (int b = 0; b < NB; ++b) Y[b] = make_float2(0.f, 0.f);
                 float e = 0.f;
                 for (int l = 0; l < L; ++l) {
-                    const float2 v = xr[s0 + l];
+                    const float2 v = X(s0 + l);
                     e += cabs2(v);
 #pragma unroll
                     for (int b = 0; b < NB; ++b) Y[b] = cadd(Y[b], cmul(Bt[b * L + l], v));
                 }
                 for (int s = s0; s < s1; ++s) {
                     if (s > s0) {
-                        const float2 dx = cscale(csub(xr[s - 1 + L], xr[s - 1]), isl);
-                        e += cabs2(xr[s - 1 + L]) - cabs2(xr[s - 1]);
+                        const float2 dx = cscale(csub(X(s - 1 + L), X(s - 1)), isl);
+                        e += cabs2(X(s - 1 + L)) - cabs2(X(s - 1));
 #pragma unroll
                         for (int b = 0; b < NB; ++b) Y[b] = cmul(rot[b], cadd(Y[b], dx));
                     }
-                    en += e;
+                    if (pass == 0) en += e;
 #pragma unroll
                     for (int i = 0; i < NB; ++i) {
-                        Yg[i] = cadd(Yg[i], Y[i]);
+                        if (pass == 0) Yg[i] = cadd(Yg[i], Y[i]);
 #pragma unroll
                         for (int j = i; j < NB; ++j) {
                             const int k = i * NB - i * (i - 1) / 2 + (j - i);
@@ -374,6 +379,10 @@ beamspace_tile_kernel(FrameDev f, float2 *__restrict__ Rbs, int tile)
                         }
                     }
                 }
+            }
+            if (f.fb) {
+#pragma unroll
+                for (int e = 0; e < NQ; ++e) P[e] = cscale(P[e], 0.5f);
             }
             // float-float reduction over the half-warp
             float2 lo[NQ];
@@ -572,6 +581,7 @@ static int launch_tile(const FrameDev &f, float2 *R_out, cudaStream_t s)
 
 int launch_beamspace(const FrameDev &f, float2 *R_out, cudaStream_t s)
 {
+    static_assert(kBeamspaceTileMaxNb == 5, "the tile kernel is instantiated for Nb = 1..5");
     switch (f.Nb) {
     case 1: return launch_tile<1>(f, R_out, s);
     case 2: return launch_tile<2>(f, R_out, s);

@@ -19,6 +19,7 @@ struct FrameDev {
     int loading;       // COS_CAPON_LOAD_*
     int r_layout;      // COS_CAPON_R_*
     int refine;
+    int fb;            // forward-backward averaged covariance
     int tile;          // pixels per range tile (kernel-specific)
     int tiles_per_beam;
     long long tile_begin;  // first global tile index of this frame
@@ -52,6 +53,12 @@ int launch_precise(const FrameDev &f, float2 *Rhi, float2 *Rlo, float *dl, float
 // Rhi + Rlo + dl; Rlo may be null) and the output stage
 int launch_precise_solve(const FrameDev &f, const float2 *Rhi, const float2 *Rlo, const float *dl, float2 *Ria,
                          unsigned *status, bool refine, cudaStream_t s);
+// forward-backward averaging in place, R = (R + J R^T J)/2, on per-pixel L x L
+// matrices (either layout; Rlo, when given, the float-float low parts)
+int launch_fb_average(const FrameDev &f, float2 *Rhi, float2 *Rlo, cudaStream_t s);
+// beamspace frames up to this many beams run the range-tile kernel (which also
+// carries forward-backward averaging)
+static constexpr int kBeamspaceTileMaxNb = 5;
 // Rhi (+ Rlo) plus the loading dl written in the frame's R layout
 int launch_format_r(const FrameDev &f, const float2 *Rhi, const float2 *Rlo, const float *dl, float2 *out,
                     cudaStream_t s);

@@ -267,6 +267,52 @@ int launch_format_r(const FrameDev &f, const float2 *Rhi, const float2 *Rlo, con
     return cudaGetLastError();
 }
 
+// Forward-backward averaging in place: (R + J R^T J)/2 maps element (a, b) to
+// the mean of R[a,b] and conj(R[L-1-a, L-1-b]), i.e. flat index i and its
+// mirror L^2-1-i in either storage order; one thread per mirror pair, the
+// pair's two new values being conjugates.  With Rlo the pair is averaged in
+// float-float (TwoSum, exact halving) and renormalised to hi + lo.
+__global__ void fb_average_kernel(long long npix, int L, float2 *__restrict__ Rhi, float2 *__restrict__ Rlo)
+{
+    const long long L2 = (long long)L * L, half = (L2 + 1) / 2;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < npix * half;
+         t += (long long)gridDim.x * blockDim.x) {
+        const long long pix = t / half, i = t % half, j = L2 - 1 - i;
+        float2 *h = Rhi + pix * L2;
+        float2 *l = Rlo ? Rlo + pix * L2 : nullptr;
+        const float2 a = h[i], b = cconj(h[j]);
+        float2 s = fadd2(a, b);
+        const float2 bb = fsub2(s, a);
+        float2 e = fadd2(fsub2(a, fsub2(s, bb)), fsub2(b, bb));
+        if (l) e = fadd2(e, fadd2(l[i], cconj(l[j])));
+        s = cscale(s, 0.5f);
+        e = cscale(e, 0.5f);
+        const float2 v = fadd2(s, e);
+        const float2 vl = fsub2(e, fsub2(v, s));
+        if (i == j) {
+            h[i] = make_float2(v.x, 0.f);
+            if (l) l[i] = make_float2(vl.x, 0.f);
+        } else {
+            h[i] = v;
+            h[j] = cconj(v);
+            if (l) {
+                l[i] = vl;
+                l[j] = cconj(vl);
+            }
+        }
+    }
+}
+
+int launch_fb_average(const FrameDev &f, float2 *Rhi, float2 *Rlo, cudaStream_t s)
+{
+    const long long npix = (long long)f.Nx * f.Npy;
+    const long long n = npix * (((long long)f.L * f.L + 1) / 2);
+    long long blocks = (n + 255) / 256;
+    if (blocks > 152 * 64) blocks = 152 * 64;
+    fb_average_kernel<<<(unsigned)blocks, 256, 0, s>>>(npix, f.L, Rhi, Rlo);
+    return cudaGetLastError();
+}
+
 int launch_precise_solve(const FrameDev &f, const float2 *Rhi, const float2 *Rlo, const float *dl, float2 *Ria,
                          unsigned *status, bool refine, cudaStream_t s)
 {
@@ -304,6 +350,7 @@ int launch_precise(const FrameDev &f, float2 *Rhi, float2 *Rlo, float *dl, float
     if (e != cudaSuccess) return e;
     precise_build_r_kernel<true><<<(unsigned)blocks, 32 * kPrecWarps, sm1, s>>>(f, Rhi, Rlo, dl);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (f.fb && (e = (cudaError_t)launch_fb_average(f, Rhi, Rlo, s)) != cudaSuccess) return e;
     return launch_precise_solve(f, Rhi, Rlo, dl, Ria, status, refine, s);
 }
 

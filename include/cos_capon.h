@@ -60,6 +60,11 @@ typedef struct cos_capon_opts {
     int r_layout;   /* COS_CAPON_R_*                                          */
     int refine;     /* 1: one step of iterative refinement of R^-1 a with an
                        FP64 residual; 0: plain FP32 Cholesky                  */
+    int fb;         /* 1: forward-backward averaged covariance (R + J R^T J)/2
+                       before loading and any beamspace transform
+                       (getCaponAllC.pyx:346-347, getCaponPy_ref.py:103-104);
+                       element space runs the float-float pipeline, beamspace
+                       supports Nb <= 5                                        */
 } cos_capon_opts;
 
 /* One frame (data cube + parameters) of a device-pointer call. */

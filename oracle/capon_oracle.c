@@ -38,6 +38,11 @@
  * convention of framework/beamformer/capon/getCaponAllC.pyx:376-385.
  * `bs_loading = 2` adds an absolute loading regCoef*I to the normalised R (no
  * reference counterpart: the form with a learnable loading scalar).
+ *
+ * Forward-backward averaging (`fb = 1`) replaces the element-space covariance
+ * by R = (R + J R^T J) / 2 before the loading and any beamspace transform
+ * (getCaponAllC.pyx:346-347; getCaponPy_ref.py:103-104;
+ * getCaponMatlab_ref.m:90-92 as R = (R + rot90(conj(R), 2)) / 2).
  */
 #define _GNU_SOURCE
 #include <complex.h>
@@ -133,7 +138,7 @@ void oracle_butler(int Nb, int L, cplx *B)
 
 typedef struct {
     const float *Xd;   /* interleaved complex64 [Nx][Ny][M] */
-    int Nx, Ny, M, L, Navg, Nb, fp32_scalars, bs_loading;
+    int Nx, Ny, M, L, Navg, Nb, fp32_scalars, bs_loading, fb;
     double regCoef;
     /* outputs (any may be NULL except z): [Nx][Ny-2Navg](...) */
     cplx *z, *zpow, *w, *R;
@@ -199,6 +204,13 @@ static void pixel_run(const job_t *jb, int x, int y, cplx *scratch)
     /* full Hermitian R (lower from upper) for the solve and the outputs */
     for (int j = 0; j < L; ++j)
         for (int k = 0; k < j; ++k) R[j * L + k] = conj(R[k * L + j]);
+
+    if (jb->fb) {   /* R = (R + J R^T J) / 2: (J R^T J)[j][k] = R[L-1-k][L-1-j] */
+        cplx *Rt = wk;
+        for (int i = 0; i < L * L; ++i) Rt[i] = R[i];
+        for (int j = 0; j < L; ++j)
+            for (int k = 0; k < L; ++k) R[j * L + k] = 0.5 * (Rt[j * L + k] + Rt[(L - 1 - k) * L + (L - 1 - j)]);
+    }
 
     cplx zz = 0, zp = 0;
     double Pv;
@@ -316,16 +328,28 @@ static void *worker(void *arg)
  * [Nx][Ny-2*Navg](...).  `nthreads` splits the beams into contiguous slabs.
  * Returns 0 on success, 1 on invalid arguments, 2 on allocation failure.
  */
+int oracle_capon_ex(const float *Xd, int Nx, int Ny, int M, double regCoef, int L, int Navg,
+                    int Nb, int bs_loading, int fp32_scalars, int fb,
+                    cplx *z, cplx *zpow, cplx *w, double *P, cplx *R, int nthreads);
+
 int oracle_capon(const float *Xd, int Nx, int Ny, int M, double regCoef, int L, int Navg,
                  int Nb, int bs_loading, int fp32_scalars,
                  cplx *z, cplx *zpow, cplx *w, double *P, cplx *R, int nthreads)
+{
+    return oracle_capon_ex(Xd, Nx, Ny, M, regCoef, L, Navg, Nb, bs_loading, fp32_scalars, 0, z, zpow, w, P, R,
+                           nthreads);
+}
+
+int oracle_capon_ex(const float *Xd, int Nx, int Ny, int M, double regCoef, int L, int Navg,
+                    int Nb, int bs_loading, int fp32_scalars, int fb,
+                    cplx *z, cplx *zpow, cplx *w, double *P, cplx *R, int nthreads)
 {
     if (Nx < 1 || Ny < 1 || L < 1 || M < 1 || Navg < 0 || Nb < 0 || L > M || Nb > L ||
         2 * Navg >= Ny || !Xd || !z)
         return 1;
     if (nthreads < 1) nthreads = 1;
     if (nthreads > Nx) nthreads = Nx;
-    job_t base = {Xd, Nx, Ny, M, L, Navg, Nb, fp32_scalars, bs_loading, regCoef,
+    job_t base = {Xd, Nx, Ny, M, L, Navg, Nb, fp32_scalars, bs_loading, fb ? 1 : 0, regCoef,
                   z, zpow, w, R, P, 0, Nx};
     if (nthreads == 1) return worker(&base) ? 2 : 0;
     pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * nthreads);

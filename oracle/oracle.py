@@ -41,6 +41,8 @@ def lib() -> C.CDLL:
         vp, i, d = C.c_void_p, C.c_int, C.c_double
         L.oracle_capon.argtypes = [vp, i, i, i, d, i, i, i, i, i, vp, vp, vp, vp, vp, i]
         L.oracle_capon.restype = i
+        L.oracle_capon_ex.argtypes = [vp, i, i, i, d, i, i, i, i, i, i, vp, vp, vp, vp, vp, i]
+        L.oracle_capon_ex.restype = i
         for name in ("oracle_cholesky",):
             getattr(L, name).argtypes = [vp, i, vp]
         for name in ("oracle_forward_solve", "oracle_back_solve"):
@@ -57,9 +59,10 @@ def _p(a):
 
 
 def capon(Xd, regCoef, L, Navg, Nb=0, bs_loading=False, fp32_scalars=True, want_w=True, want_R=False,
-          nthreads=1, absolute=False) -> dict:
+          nthreads=1, absolute=False, fb=False) -> dict:
     """absolute=True: R_d = R + regCoef*I on the normalised R instead of the
-    relative loading regCoef*tr(R)/L."""
+    relative loading regCoef*tr(R)/L.  fb=True: forward-backward averaged
+    covariance (R + J R^T J)/2 before loading and any beamspace transform."""
     Xd = np.ascontiguousarray(Xd, dtype=np.complex64)
     Nx, Ny, M = Xd.shape
     npy = Ny - 2 * Navg
@@ -71,9 +74,9 @@ def capon(Xd, regCoef, L, Navg, Nb=0, bs_loading=False, fp32_scalars=True, want_
         R=np.zeros((Nx, npy, L, L), np.complex128) if want_R else None,
     )
     mode = 2 if absolute else int(bool(bs_loading))
-    rc = lib().oracle_capon(_p(Xd), Nx, Ny, M, float(regCoef), int(L), int(Navg), int(Nb), mode,
-                            int(bool(fp32_scalars)), _p(out["z"]), _p(out["zpow"]), _p(out["w"]), _p(out["P"]),
-                            _p(out["R"]), int(nthreads))
+    rc = lib().oracle_capon_ex(_p(Xd), Nx, Ny, M, float(regCoef), int(L), int(Navg), int(Nb), mode,
+                               int(bool(fp32_scalars)), int(bool(fb)), _p(out["z"]), _p(out["zpow"]), _p(out["w"]),
+                               _p(out["P"]), _p(out["R"]), int(nthreads))
     if rc != 0:
         raise ValueError(f"oracle_capon returned {rc}")
     return out

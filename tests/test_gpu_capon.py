@@ -329,3 +329,49 @@ def test_multi_frame_cuda_graph(cap):
         torch.cuda.synchronize()
         for f, (z0, P0) in zip(frames, eager):
             assert torch.equal(f.z, z0) and torch.equal(f.P, P0)
+
+
+@pytest.mark.parametrize("form,tol", [(0, TOL_P), (1, TOL_P_PLAIN), (4, 1e-4)])
+def test_forward_backward_averaging_element_space(cap, form, tol):
+    """FB averaging (R + J R^T J)/2 against the oracle: the default form runs
+    the float-float pipeline, the plain FP32 form and the TF32x3 tensor-core
+    form average their own R; R output is the averaged matrix."""
+    from cos_gb300 import _lib, synth
+    x = synth.cube(40, 4, 64, [10.0, 5.0], seed=21)
+    ref = oracle.capon(x, 0.01, 32, 2, want_R=True, fb=True, nthreads=4)
+    Nx, Ny, M = x.shape
+    npy = Ny - 4
+    z = np.zeros((Nx, npy), np.complex64)
+    P = np.zeros((Nx, npy), np.float32)
+    w = np.zeros((Nx, npy, 32), np.complex64)
+    R = np.zeros((Nx, npy, 32, 32), np.complex64)
+    o = cap.opts(form=form, fb=1, r_layout=_lib.R_NORMALISED)
+    assert cap.Capon().getCaponEx(z, P, w, R, x, 0.01, 32, 2, M, Nx, Ny, 0, o) == 0
+    eP = (np.abs(P - ref["P"]) / ref["P"]).max()
+    eR = np.abs(R - ref["R"]).max() / np.abs(ref["R"]).max()
+    plain = oracle.capon(x, 0.01, 32, 2, nthreads=4)
+    assert (np.abs(plain["P"] - ref["P"]) / ref["P"]).max() > 10 * tol   # FB changes the answer here
+    print(f"form {form} fb: P {eP:.2e} R {eR:.2e}")
+    assert eP < tol and eR < 1e-5
+    # R is persymmetric: R[a,b] = conj(R[L-1-a, L-1-b])
+    np.testing.assert_allclose(R, np.conj(R[:, :, ::-1, ::-1]), rtol=0, atol=1e-6 * np.abs(R).max())
+
+
+@pytest.mark.parametrize("bs_loading", [0, 1])
+@pytest.mark.parametrize("M,L,Nb", [(96, 48, 3), (128, 64, 5), (32, 16, 4)])
+def test_forward_backward_averaging_beamspace(cap, M, L, Nb, bs_loading):
+    from cos_gb300 import synth
+    x = synth.cube(48, 4, M, [10.0, 5.0], seed=M + 3 * Nb)
+    V = np.zeros((Nb, L))
+    z, P, w = cap.getCaponGPU(x, 0.01, L, 1, V, doFBAvg=True, loading=bs_loading)
+    ref = oracle.capon(x, 0.01, L, 1, Nb=Nb, bs_loading=bool(bs_loading), fb=True, nthreads=4)
+    assert_close(z, P, w, ref, what=f"FB beamspace M{M} L{L} Nb{Nb} load{bs_loading}")
+
+
+def test_forward_backward_averaging_unsupported_beams(cap):
+    from cos_gb300 import _lib
+    x = np.zeros((2, 20, 32), np.complex64)
+    z = np.zeros((2, 18), np.complex64)
+    P = np.zeros((2, 18), np.float32)
+    e = cap.Capon().getCaponEx(z, P, None, None, x, 0.01, 16, 1, 32, 2, 20, 7, cap.opts(fb=1))
+    assert e == _lib.ERR_NOT_SUPPORTED

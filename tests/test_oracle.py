@@ -148,3 +148,53 @@ def test_reference_cpu_path_live():
     o = oracle.capon(x, 0.02, 7, 2)
     np.testing.assert_allclose(o["z"], zr, rtol=1e-10, atol=1e-13)
     np.testing.assert_allclose(o["w"], wr, rtol=1e-9, atol=1e-12)
+
+
+def _numpy_capon_fb(x, regCoef, L, K, fb):
+    """Per-pixel restatement of getCaponPy_ref.py:86-121 (R from the snapshot
+    matrix d, optional R = (R + J R^T J)/2, loading regCoef*tr(R)/L, w, z, P)."""
+    Nx, Ny, M = x.shape
+    Ns, T = M - L + 1, 2 * K + 1
+    J = np.fliplr(np.eye(L))
+    out = np.zeros((Nx, Ny - 2 * K)), np.zeros((Nx, Ny - 2 * K), complex)
+    for b in range(Nx):
+        for p in range(Ny - 2 * K):
+            d = np.array([x[b, p + t, s:s + L] for t in range(T) for s in range(Ns)]).astype(complex)
+            R = d.T @ d.conj() / (Ns * T)          # R[j,k] = sum x[s+j] conj(x[s+k])
+            if fb:
+                R = 0.5 * (R + J @ R.T @ J)
+            g = x[b, p + K].astype(complex)
+            g = np.array([g[l:l + Ns].sum() for l in range(L)]) / Ns
+            Rd = R + regCoef * np.trace(R) / L * np.eye(L)
+            Ria = np.linalg.solve(Rd, np.ones(L))
+            w = Ria / Ria.sum()
+            out[0][b, p] = 1.0 / Ria.sum().real
+            out[1][b, p] = np.vdot(w, g)
+    return out
+
+
+@pytest.mark.parametrize("fb", [False, True])
+def test_forward_backward_averaging_matches_numpy_restatement(fb):
+    rng = np.random.default_rng(11)
+    x = (rng.standard_normal((2, 10, 12)) + 1j * rng.standard_normal((2, 10, 12))).astype(np.complex64)
+    x[:, :, :] += 4.0 * np.exp(1j * 0.9 * np.arange(12))
+    P, z = _numpy_capon_fb(x, 0.05, 5, 1, fb)
+    o = oracle.capon(x, 0.05, 5, 1, fb=fb, fp32_scalars=False)
+    np.testing.assert_allclose(o["P"], P, rtol=1e-10)
+    np.testing.assert_allclose(o["z"], z, rtol=1e-9, atol=1e-12)
+    if fb:  # the averaging changes the answer on this (non-persymmetric) data
+        o0 = oracle.capon(x, 0.05, 5, 1, fp32_scalars=False)
+        assert np.abs(o0["P"] - o["P"]).max() > 1e-6 * np.abs(o["P"]).max()
+
+
+def test_forward_backward_equals_flipped_conjugate_rows():
+    """(R + J R^T J)/2 is the mean of the covariances of x and of
+    x~[m] = conj(x[M-1-m]) -- the identity the beamspace kernel uses."""
+    rng = np.random.default_rng(12)
+    x = (rng.standard_normal((2, 9, 14)) + 1j * rng.standard_normal((2, 9, 14))).astype(np.complex64)
+    L, K = 6, 1
+    a = oracle.capon(x, 0.0, L, K, want_R=True, fb=True, fp32_scalars=False)["R"]
+    xt = np.ascontiguousarray(np.conj(x[:, :, ::-1]))
+    r0 = oracle.capon(x, 0.0, L, K, want_R=True, fp32_scalars=False)["R"]
+    r1 = oracle.capon(xt, 0.0, L, K, want_R=True, fp32_scalars=False)["R"]
+    np.testing.assert_allclose(a, 0.5 * (r0 + r1), rtol=1e-12, atol=1e-12)
