@@ -27,7 +27,7 @@ EXPORTS = (
     "cos_capon_create", "cos_capon_destroy", "cos_capon_get_capon", "cos_capon_get_capon_ex",
     "cos_capon_run", "cos_capon_build_r", "cos_capon_solve", "cos_capon_butler",
     "cos_capon_device_status", "cos_capon_status_string", "cos_capon_run_plain_noalloc",
-    "cos_capon_backward",
+    "cos_capon_backward", "cos_capon_get_capon_subspace",
 )
 
 
@@ -40,7 +40,7 @@ class Frame(C.Structure):
     _fields_ = [
         ("x", C.c_void_p), ("z", C.c_void_p), ("P", C.c_void_p), ("w", C.c_void_p), ("R", C.c_void_p),
         ("d", C.c_float), ("L", C.c_int), ("K", C.c_int), ("M", C.c_int), ("Nx", C.c_int),
-        ("Ny", C.c_int), ("Nb", C.c_int),
+        ("Ny", C.c_int), ("Nb", C.c_int), ("V", C.c_void_p),
     ]
 
 
@@ -75,6 +75,7 @@ def _load() -> C.CDLL:
         "cos_capon_status_string": [i],
         "cos_capon_run_plain_noalloc": [C.POINTER(Frame), vp],
         "cos_capon_backward": [vp, C.POINTER(Adjoint), vp],
+        "cos_capon_get_capon_subspace": [vp, vp, vp, vp, vp, vp, f, i, i, i, i, i, i, C.POINTER(Opts)],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)

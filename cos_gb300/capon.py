@@ -133,11 +133,14 @@ def getCaponCUDAPy(Xd, d, L, Navg, V, doFBAvg=False, verbose=False, want_R: bool
 
 
 def getCaponGPU(Xd, regCoef, L, Navg, V=None, doFBAvg=False, verbose=False, *, form=_lib.FORM_FUSED,
-                loading=_lib.LOAD_ELEMENT, want_w: bool = True):
+                loading=_lib.LOAD_ELEMENT, want_w: bool = True, subspace=None):
     """getCaponCPy argument order on the GPU path: returns [z, P, w]
     (complex64 z, float32 P, complex64 w or None).  doFBAvg applies
     forward-backward averaging (the reference CPU path accepts the flag and
     ignores it, getCaponC.pyx:106; its definition is getCaponAllC.pyx:346-347).
+    V, as in the reference GPU path, gives only the beam count Nb = V.shape[0]
+    (the Butler matrix is used); `subspace` (complex [Nb][L]) is a caller-given
+    subspace matrix with getCaponAllC.pyx:226-231, 365-370 semantics.
     Raises CaponError on a nonzero status."""
     Xd = np.ascontiguousarray(Xd, dtype=np.complex64)
     Nx, Ny, M = Xd.shape
@@ -146,6 +149,16 @@ def getCaponGPU(Xd, regCoef, L, Navg, V=None, doFBAvg=False, verbose=False, *, f
     z = np.zeros((Nx, Ny - 2 * Navg), np.complex64)
     P = np.zeros((Nx, Ny - 2 * Navg), np.float32)
     w = np.zeros((Nx, Ny - 2 * Navg, L), np.complex64) if want_w else None
+    if subspace is not None:
+        Vs = np.ascontiguousarray(subspace, dtype=np.complex64)
+        if Vs.ndim != 2 or Vs.shape[1] != L:
+            raise ValueError("subspace must be [Nb][L]")
+        o = opts(form=form, loading=loading, fb=int(bool(doFBAvg)))
+        check(lib.cos_capon_get_capon_subspace(_module_ctx().handle, _ptr(z), _ptr(P),
+                                               _ptr(w) if w is not None else None, _ptr(Xd), _ptr(Vs),
+                                               float(regCoef), L, Navg, M, Nx, Ny, int(Vs.shape[0]), C.byref(o)),
+              "cos_capon_get_capon_subspace")
+        return [z, P, w]
     check(_module_ctx().getCaponEx(z, P, w, None, Xd, float(regCoef), L, Navg, M, Nx, Ny, Nb,
                                    opts(form=form, loading=loading, fb=int(bool(doFBAvg)))),
           "cos_capon_get_capon_ex")
@@ -164,13 +177,14 @@ class DeviceFrame:
     P: object = None          # float32 [Nx][Ny-2K] or None
     w: object = None          # complex64 [Nx][Ny-2K][L] or None
     R: object = None          # complex64 [Nx][Ny-2K][L][L] or None
+    V: object = None          # complex64 [Nb][L] subspace matrix or None (Butler)
 
     def ctypes_frame(self) -> Frame:
         Nx, Ny, M = self.x.shape
         def p(t):
             return t.data_ptr() if t is not None else None
         return Frame(p(self.x), p(self.z), p(self.P), p(self.w), p(self.R), float(self.d), int(self.L),
-                     int(self.K), int(M), int(Nx), int(Ny), int(self.Nb))
+                     int(self.K), int(M), int(Nx), int(Ny), int(self.Nb), p(self.V))
 
 
 def capon_frames(frames: Sequence[DeviceFrame], ctx: Optional[Context] = None, o: Optional[Opts] = None,

@@ -57,6 +57,7 @@ struct cos_capon_ctx {
     DevBuf Rwork, Rlo, dl, Ria;
     // stage entry points
     DevBuf A, b, sol;
+    DevBuf V;           // subspace matrix of the host-pointer subspace call
     // autotuner: chosen fused candidate per (L, K, M, w-or-R requested)
     std::map<std::tuple<int, int, int, int>, int> tuned;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -106,6 +107,7 @@ static FrameDev make_frame(const cos_capon_frame &fr, const cos_capon_opts &o)
     f.Nx = fr.Nx;
     f.Ny = fr.Ny;
     f.Nb = fr.Nb;
+    f.V = fr.Nb > 0 ? (const float2 *)fr.V : nullptr;
     f.Npy = fr.Ny - 2 * fr.K;
     f.loading = o.loading;
     f.r_layout = o.r_layout;
@@ -371,7 +373,7 @@ int cos_capon_destroy(cos_capon_ctx *c)
     if (!c) return COS_CAPON_ERR_INVALID_VALUE;
     cudaStreamSynchronize(c->stream);
     for (DevBuf *b : {&c->x, &c->z, &c->P, &c->w, &c->R, &c->Rwork, &c->Rlo, &c->dl, &c->Ria, &c->A, &c->b,
-                      &c->sol})
+                      &c->sol, &c->V})
         b->release();
     if (c->d_status) cudaFree(c->d_status);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -402,13 +404,15 @@ int cos_capon_run(cos_capon_ctx *c, const cos_capon_frame *frames, int nframes, 
     return run_frames(c, fs.data(), nframes, o, s);
 }
 
-int cos_capon_get_capon_ex(cos_capon_ctx *c, void *z, float *P, void *w, void *R, const void *x, float d, int L,
-                           int Yavg, int M, int Nx, int Nz, int Nb, const cos_capon_opts *opts)
+// the host-pointer call; V (host, [Nb][L]) selects a caller-given subspace
+static int get_capon_host(cos_capon_ctx *c, void *z, float *P, void *w, void *R, const void *x, const void *V,
+                          float d, int L, int Yavg, int M, int Nx, int Nz, int Nb, const cos_capon_opts *opts)
 {
     if (!c) return COS_CAPON_ERR_INVALID_VALUE;
     int e = check_sizes(L, Yavg, M, Nx, Nz, Nb);
     if (e) return e;
     if (!x || !z) return COS_CAPON_ERR_INVALID_VALUE;
+    if (V && Nb < 1) return COS_CAPON_ERR_INVALID_VALUE;
     const cos_capon_opts o = opts ? *opts : kDefaultOpts;
     const size_t N = (size_t)Nx * Nz, npix = (size_t)Nx * (Nz - 2 * Yavg);
     const size_t bx = N * M * sizeof(float2), bz = npix * sizeof(float2), bp = npix * sizeof(float),
@@ -438,6 +442,13 @@ int cos_capon_get_capon_ex(cos_capon_ctx *c, void *z, float *P, void *w, void *R
 
     cudaStream_t s = c->stream;
     cudaError_t ce;
+    const void *Vd = nullptr;
+    if (V) {
+        const size_t bv = (size_t)Nb * L * sizeof(float2);
+        if ((e = c->V.ensure(bv))) return e;
+        if ((ce = cudaMemcpyAsync(c->V.p, V, bv, cudaMemcpyHostToDevice, s)) != cudaSuccess) return ce;
+        Vd = c->V.p;
+    }
     // Pinned host buffers and a path without shared scratch (fused, beamspace):
     // split the beams into chunks on two streams so that the copies of one
     // chunk overlap the kernel of the other.  The first call of a fused shape
@@ -445,7 +456,7 @@ int cos_capon_get_capon_ex(cos_capon_ctx *c, void *z, float *P, void *w, void *R
     const bool fused = use_fused(make_frame(probe, o), o);
     const bool no_scratch = fused || Nb > 0;
     const bool tuned = !fused || c->tuned.count(std::make_tuple(L, Yavg, M, (int)(w != nullptr || R != nullptr)));
-    if (no_scratch && tuned && !R && Nx >= 4 && is_pinned(x) && is_pinned(z) && (!P || is_pinned(P)) &&
+    if (no_scratch && tuned && !R && !V && Nx >= 4 && is_pinned(x) && is_pinned(z) && (!P || is_pinned(P)) &&
         (!w || is_pinned(w))) {
         if (!c->stream2 && cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking) != cudaSuccess) {
             cudaGetLastError();
@@ -491,6 +502,8 @@ int cos_capon_get_capon_ex(cos_capon_ctx *c, void *z, float *P, void *w, void *R
     }
     if ((ce = cudaMemcpyAsync(c->x.p, x, bx, cudaMemcpyHostToDevice, s)) != cudaSuccess) return ce;
     cos_capon_frame fr;
+    memset(&fr, 0, sizeof(fr));
+    fr.V = Vd;
     fr.x = c->x.p;
     fr.z = c->z.p;
     fr.P = P ? (float *)c->P.p : nullptr;
@@ -509,6 +522,19 @@ int cos_capon_get_capon_ex(cos_capon_ctx *c, void *z, float *P, void *w, void *R
     if (w && (ce = cudaMemcpyAsync(w, c->w.p, bw, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return ce;
     if (R && (ce = cudaMemcpyAsync(R, c->R.p, bR, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return ce;
     return read_status(c, s, true);
+}
+
+int cos_capon_get_capon_ex(cos_capon_ctx *c, void *z, float *P, void *w, void *R, const void *x, float d, int L,
+                           int Yavg, int M, int Nx, int Nz, int Nb, const cos_capon_opts *opts)
+{
+    return get_capon_host(c, z, P, w, R, x, nullptr, d, L, Yavg, M, Nx, Nz, Nb, opts);
+}
+
+int cos_capon_get_capon_subspace(cos_capon_ctx *c, void *z, float *P, void *w, const void *x, const void *V, float d,
+                                 int L, int Yavg, int M, int Nx, int Nz, int Nb, const cos_capon_opts *opts)
+{
+    if (!V) return COS_CAPON_ERR_INVALID_VALUE;
+    return get_capon_host(c, z, P, w, nullptr, x, V, d, L, Yavg, M, Nx, Nz, Nb, opts);
 }
 
 int cos_capon_get_capon(cos_capon_ctx *c, void *z, void *w, void *R, const void *x, float d, int L, int Yavg, int M,

@@ -268,7 +268,7 @@ struct BsTile {
 
 struct BsTileSmem {
     int rows, tile;
-    size_t off_x, off_q, off_e, off_g, off_b, off_xs, total;
+    size_t off_x, off_q, off_e, off_g, off_b, off_xs, off_vv, total;
     __host__ __device__ BsTileSmem(int tile_, int K, int M, int L, int NB)
     {
         tile = tile_;
@@ -280,7 +280,8 @@ struct BsTileSmem {
         off_g = off_e + (((size_t)rows * sizeof(float) + 15) & ~(size_t)15); // rows x NB: beam sums
         off_b = off_g + (size_t)rows * NB * sizeof(float2);                 // Butler NB x L, rot NB, a_bs NB
         off_xs = off_b + (size_t)(NB * L + 2 * NB) * sizeof(float2);        // tile x (NB + 1): x_bs, 1/sum
-        total = off_xs + (size_t)tile * (NB + 1) * sizeof(float2);
+        off_vv = off_xs + (size_t)tile * (NB + 1) * sizeof(float2);          // NQ: V V^H (packed upper)
+        total = off_vv + (size_t)NQ * sizeof(float2);
     }
 };
 
@@ -300,8 +301,13 @@ beamspace_tile_kernel(FrameDev f, float2 *__restrict__ Rbs, int tile)
     float2 *rot = Bt + NB * L;
     float2 *ab = rot + NB;
     float2 *Xb = (float2 *)(smraw + S.off_xs);
+    float2 *VV = (float2 *)(smraw + S.off_vv);
     const int tid = threadIdx.x;
     const float isl = 1.0f / sqrtf((float)L);
+    // a caller-given subspace V: direct products per subarray (no sliding
+    // recurrence) and element-space loadings enter as dl V V^H
+    const bool direct = f.V != nullptr;
+    const bool loadVV = direct && f.loading != COS_CAPON_LOAD_BEAMSPACE;
 
     const int tiles_per_beam = (f.Npy + tile - 1) / tile;
     const int bx = blockIdx.x / tiles_per_beam;
@@ -309,12 +315,16 @@ beamspace_tile_kernel(FrameDev f, float2 *__restrict__ Rbs, int tile)
     const int np = min(tile, f.Npy - p0);
     const int rows = np + 2 * K;
 
-    // Butler table and the a_bs = B 1 of this launch
+    // Butler table (or the caller's V) and the a_bs = B 1 of this launch
     for (int i = tid; i < NB * L; i += kTileThreads) {
-        const int bb = i / L, l = i % L;
-        float sn, cs;
-        sincospif(2.0f * (float)((butler_bin(bb, NB, L) * l) % L) / (float)L, &sn, &cs);
-        Bt[i] = make_float2(cs * isl, -sn * isl);
+        if (direct) {
+            Bt[i] = f.V[i];
+        } else {
+            const int bb = i / L, l = i % L;
+            float sn, cs;
+            sincospif(2.0f * (float)((butler_bin(bb, NB, L) * l) % L) / (float)L, &sn, &cs);
+            Bt[i] = make_float2(cs * isl, -sn * isl);
+        }
     }
     if (tid < NB) {
         float sn, cs;
@@ -329,6 +339,17 @@ beamspace_tile_kernel(FrameDev f, float2 *__restrict__ Rbs, int tile)
         float2 acc = make_float2(0.f, 0.f);
         for (int l = 0; l < L; ++l) acc = cadd(acc, Bt[tid * L + l]);
         ab[tid] = acc;
+    }
+    if (loadVV && tid < BsTile<NB>::NQ) {
+        int i = 0, rem = tid;
+        while (rem >= NB - i) {
+            rem -= NB - i;
+            ++i;
+        }
+        const int j = i + rem;
+        float2 acc = make_float2(0.f, 0.f);
+        for (int l = 0; l < L; ++l) acc = cadd(acc, cmulc(Bt[i * L + l], Bt[j * L + l]));
+        VV[tid] = acc;
     }
 
     // ---- phase A: per-row terms, one half-warp per row
@@ -363,10 +384,20 @@ beamspace_tile_kernel(FrameDev f, float2 *__restrict__ Rbs, int tile)
                 }
                 for (int s = s0; s < s1; ++s) {
                     if (s > s0) {
-                        const float2 dx = cscale(csub(X(s - 1 + L), X(s - 1)), isl);
                         e += cabs2(X(s - 1 + L)) - cabs2(X(s - 1));
+                        if (direct) {
 #pragma unroll
-                        for (int b = 0; b < NB; ++b) Y[b] = cmul(rot[b], cadd(Y[b], dx));
+                            for (int b = 0; b < NB; ++b) Y[b] = make_float2(0.f, 0.f);
+                            for (int l = 0; l < L; ++l) {
+                                const float2 v = X(s + l);
+#pragma unroll
+                                for (int b = 0; b < NB; ++b) Y[b] = cadd(Y[b], cmul(Bt[b * L + l], v));
+                            }
+                        } else {
+                            const float2 dx = cscale(csub(X(s - 1 + L), X(s - 1)), isl);
+#pragma unroll
+                            for (int b = 0; b < NB; ++b) Y[b] = cmul(rot[b], cadd(Y[b], dx));
+                        }
                     }
                     if (pass == 0) en += e;
 #pragma unroll
@@ -462,7 +493,8 @@ beamspace_tile_kernel(FrameDev f, float2 *__restrict__ Rbs, int tile)
             for (int i = 0; i < NB; ++i)
 #pragma unroll
                 for (int j = i; j < NB; ++j, ++k) {
-                    const float2 v = (i == j) ? make_float2(Rh[k].x + dl, 0.f) : Rh[k];
+                    const float2 v = loadVV ? cadd(Rh[k], cscale(VV[k], dl))
+                                            : ((i == j) ? make_float2(Rh[k].x + dl, 0.f) : Rh[k]);
                     Rp[i + j * NB] = v;
                     if (i != j) Rp[j + i * NB] = cconj(v);
                 }
@@ -474,7 +506,8 @@ beamspace_tile_kernel(FrameDev f, float2 *__restrict__ Rbs, int tile)
 #pragma unroll
             for (int i = 0; i < NB; ++i)
 #pragma unroll
-                for (int j = i; j < NB; ++j, ++k) U[k] = (i == j) ? make_float2(Rh[k].x + dl, 0.f) : Rh[k];
+                for (int j = i; j < NB; ++j, ++k)
+                    U[k] = loadVV ? cadd(Rh[k], cscale(VV[k], dl)) : ((i == j) ? make_float2(Rh[k].x + dl, 0.f) : Rh[k]);
         }
         auto idx = [](int i, int j) { return i * NB - i * (i - 1) / 2 + (j - i); };   // i <= j
 #pragma unroll
@@ -519,12 +552,23 @@ beamspace_tile_kernel(FrameDev f, float2 *__restrict__ Rbs, int tile)
                 double ar, ai;
                 if (i <= j) {
                     const int k = idx(i, j);
-                    ar = (double)Rh[k].x + (double)Rl[k].x + (i == j ? (double)dl : 0.0);
-                    ai = (i == j) ? 0.0 : (double)Rh[k].y + (double)Rl[k].y;
+                    ar = (double)Rh[k].x + (double)Rl[k].x;
+                    ai = (double)Rh[k].y + (double)Rl[k].y;
+                    if (loadVV) {
+                        ar += (double)dl * (double)VV[k].x;
+                        ai += (double)dl * (double)VV[k].y;
+                    } else if (i == j) {
+                        ar += (double)dl;
+                    }
+                    if (i == j) ai = 0.0;
                 } else {
                     const int k = idx(j, i);
                     ar = (double)Rh[k].x + (double)Rl[k].x;
                     ai = -((double)Rh[k].y + (double)Rl[k].y);
+                    if (loadVV) {
+                        ar += (double)dl * (double)VV[k].x;
+                        ai -= (double)dl * (double)VV[k].y;
+                    }
                 }
                 rr -= ar * (double)xb[j].x - ai * (double)xb[j].y;
                 ri -= ar * (double)xb[j].y + ai * (double)xb[j].x;
@@ -582,6 +626,7 @@ static int launch_tile(const FrameDev &f, float2 *R_out, cudaStream_t s)
 int launch_beamspace(const FrameDev &f, float2 *R_out, cudaStream_t s)
 {
     static_assert(kBeamspaceTileMaxNb == 5, "the tile kernel is instantiated for Nb = 1..5");
+    if (f.V && f.Nb > kBeamspaceTileMaxNb) return cudaErrorNotSupported;
     switch (f.Nb) {
     case 1: return launch_tile<1>(f, R_out, s);
     case 2: return launch_tile<2>(f, R_out, s);

@@ -20,6 +20,7 @@ struct FrameDev {
     int r_layout;      // COS_CAPON_R_*
     int refine;
     int fb;            // forward-backward averaged covariance
+    const float2 *V;   // [Nb][L] beamspace subspace matrix, null = Butler
     int tile;          // pixels per range tile (kernel-specific)
     int tiles_per_beam;
     long long tile_begin;  // first global tile index of this frame

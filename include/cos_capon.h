@@ -81,6 +81,11 @@ typedef struct cos_capon_frame {
     int Nx;         /* beams                                                  */
     int Ny;         /* range samples                                          */
     int Nb;         /* beamspace dimension, 0 = element space                 */
+    const void *V;  /* device, complex64 [Nb][L] subspace matrix (row-major)
+                       for beamspace, or NULL for the Butler matrix of the
+                       reference GPU path (capon_kernel.cu:47-77); a general V
+                       follows getCaponAllC.pyx:226-231, 365-370:
+                       a_bs = V 1, R_bs = V R V^H, g_bs = V g                 */
 } cos_capon_frame;
 
 typedef struct cos_capon_ctx cos_capon_ctx;
@@ -107,6 +112,16 @@ int cos_capon_get_capon(cos_capon_ctx *ctx, void *z, void *w, void *R, const voi
 int cos_capon_get_capon_ex(cos_capon_ctx *ctx, void *z, float *P, void *w, void *R,
                            const void *x, float d, int L, int Yavg, int M, int Nx, int Nz,
                            int Nb, const cos_capon_opts *opts);
+
+/* Beamspace with a caller-given subspace matrix V (host, complex64 [Nb][L],
+ * row-major): getCaponAllC.pyx:226-231, 365-370 semantics.  Element-space
+ * loading becomes d tr(R)/L V V^H in beamspace (the reference loads R before
+ * the transform).  w is the element-space weight V^H x_bs / (a_bs^H x_bs).
+ * No reference GPU counterpart (its beamspace route always uses the Butler
+ * matrix).  Host pointers, synchronous. */
+int cos_capon_get_capon_subspace(cos_capon_ctx *ctx, void *z, float *P, void *w, const void *x, const void *V,
+                                 float d, int L, int Yavg, int M, int Nx, int Nz, int Nb,
+                                 const cos_capon_opts *opts);
 
 /* Device-pointer call: every pixel of `nframes` frames (each with its own M, L,
  * K, Nb) in one launch on `stream` (a cudaStream_t; NULL = the default stream).  Asynchronous; no host synchronisation and no allocation once the

@@ -140,6 +140,7 @@ typedef struct {
     const float *Xd;   /* interleaved complex64 [Nx][Ny][M] */
     int Nx, Ny, M, L, Navg, Nb, fp32_scalars, bs_loading, fb;
     double regCoef;
+    const cplx *V;     /* Nb x L subspace matrix (row-major) or NULL for the Butler matrix */
     /* outputs (any may be NULL except z): [Nx][Ny-2Navg](...) */
     cplx *z, *zpow, *w, *R;
     double *P;
@@ -243,7 +244,10 @@ static void pixel_run(const job_t *jb, int x, int y, cplx *scratch)
         cplx *ab = tmp + (size_t)Nb * L;               /* Nb */
         cplx *xb = ab + Nb;                            /* Nb */
         cplx *wb = xb + Nb;                            /* 2 Nb Nb + Nb */
-        oracle_butler(Nb, L, B);
+        if (jb->V) /* a given subspace (getCaponAllC.pyx:226-231, 365-370) */
+            for (int i = 0; i < Nb * L; ++i) B[i] = jb->V[i];
+        else
+            oracle_butler(Nb, L, B);
         if (jb->bs_loading != 1) {
             cplx tr = 0;
             for (int i = 0; i < L; ++i) tr += R[i * L + i];
@@ -328,9 +332,17 @@ static void *worker(void *arg)
  * [Nx][Ny-2*Navg](...).  `nthreads` splits the beams into contiguous slabs.
  * Returns 0 on success, 1 on invalid arguments, 2 on allocation failure.
  */
+int oracle_capon_v(const float *Xd, int Nx, int Ny, int M, double regCoef, int L, int Navg,
+                   int Nb, int bs_loading, int fp32_scalars, int fb, const cplx *V,
+                   cplx *z, cplx *zpow, cplx *w, double *P, cplx *R, int nthreads);
+
 int oracle_capon_ex(const float *Xd, int Nx, int Ny, int M, double regCoef, int L, int Navg,
                     int Nb, int bs_loading, int fp32_scalars, int fb,
-                    cplx *z, cplx *zpow, cplx *w, double *P, cplx *R, int nthreads);
+                    cplx *z, cplx *zpow, cplx *w, double *P, cplx *R, int nthreads)
+{
+    return oracle_capon_v(Xd, Nx, Ny, M, regCoef, L, Navg, Nb, bs_loading, fp32_scalars, fb, NULL, z, zpow, w, P,
+                          R, nthreads);
+}
 
 int oracle_capon(const float *Xd, int Nx, int Ny, int M, double regCoef, int L, int Navg,
                  int Nb, int bs_loading, int fp32_scalars,
@@ -340,16 +352,18 @@ int oracle_capon(const float *Xd, int Nx, int Ny, int M, double regCoef, int L, 
                            nthreads);
 }
 
-int oracle_capon_ex(const float *Xd, int Nx, int Ny, int M, double regCoef, int L, int Navg,
-                    int Nb, int bs_loading, int fp32_scalars, int fb,
-                    cplx *z, cplx *zpow, cplx *w, double *P, cplx *R, int nthreads)
+/* Nb > 0 with V != NULL: beamspace over the given subspace (V B^H-style
+ * transform of the loaded element-space R; a_bs = V 1; w = V^H x_bs / a_bs^H x_bs) */
+int oracle_capon_v(const float *Xd, int Nx, int Ny, int M, double regCoef, int L, int Navg,
+                   int Nb, int bs_loading, int fp32_scalars, int fb, const cplx *V,
+                   cplx *z, cplx *zpow, cplx *w, double *P, cplx *R, int nthreads)
 {
     if (Nx < 1 || Ny < 1 || L < 1 || M < 1 || Navg < 0 || Nb < 0 || L > M || Nb > L ||
         2 * Navg >= Ny || !Xd || !z)
         return 1;
     if (nthreads < 1) nthreads = 1;
     if (nthreads > Nx) nthreads = Nx;
-    job_t base = {Xd, Nx, Ny, M, L, Navg, Nb, fp32_scalars, bs_loading, fb ? 1 : 0, regCoef,
+    job_t base = {Xd, Nx, Ny, M, L, Navg, Nb, fp32_scalars, bs_loading, fb ? 1 : 0, regCoef, V,
                   z, zpow, w, R, P, 0, Nx};
     if (nthreads == 1) return worker(&base) ? 2 : 0;
     pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * nthreads);

@@ -43,6 +43,8 @@ def lib() -> C.CDLL:
         L.oracle_capon.restype = i
         L.oracle_capon_ex.argtypes = [vp, i, i, i, d, i, i, i, i, i, i, vp, vp, vp, vp, vp, i]
         L.oracle_capon_ex.restype = i
+        L.oracle_capon_v.argtypes = [vp, i, i, i, d, i, i, i, i, i, i, vp, vp, vp, vp, vp, vp, i]
+        L.oracle_capon_v.restype = i
         for name in ("oracle_cholesky",):
             getattr(L, name).argtypes = [vp, i, vp]
         for name in ("oracle_forward_solve", "oracle_back_solve"):
@@ -59,10 +61,11 @@ def _p(a):
 
 
 def capon(Xd, regCoef, L, Navg, Nb=0, bs_loading=False, fp32_scalars=True, want_w=True, want_R=False,
-          nthreads=1, absolute=False, fb=False) -> dict:
+          nthreads=1, absolute=False, fb=False, V=None) -> dict:
     """absolute=True: R_d = R + regCoef*I on the normalised R instead of the
     relative loading regCoef*tr(R)/L.  fb=True: forward-backward averaged
-    covariance (R + J R^T J)/2 before loading and any beamspace transform."""
+    covariance (R + J R^T J)/2 before loading and any beamspace transform.
+    V: optional Nb x L subspace matrix replacing the Butler matrix (Nb > 0)."""
     Xd = np.ascontiguousarray(Xd, dtype=np.complex64)
     Nx, Ny, M = Xd.shape
     npy = Ny - 2 * Navg
@@ -74,9 +77,10 @@ def capon(Xd, regCoef, L, Navg, Nb=0, bs_loading=False, fp32_scalars=True, want_
         R=np.zeros((Nx, npy, L, L), np.complex128) if want_R else None,
     )
     mode = 2 if absolute else int(bool(bs_loading))
-    rc = lib().oracle_capon_ex(_p(Xd), Nx, Ny, M, float(regCoef), int(L), int(Navg), int(Nb), mode,
-                               int(bool(fp32_scalars)), int(bool(fb)), _p(out["z"]), _p(out["zpow"]), _p(out["w"]),
-                               _p(out["P"]), _p(out["R"]), int(nthreads))
+    Vc = None if V is None else np.ascontiguousarray(V, dtype=np.complex128)
+    rc = lib().oracle_capon_v(_p(Xd), Nx, Ny, M, float(regCoef), int(L), int(Navg), int(Nb), mode,
+                              int(bool(fp32_scalars)), int(bool(fb)), _p(Vc), _p(out["z"]), _p(out["zpow"]),
+                              _p(out["w"]), _p(out["P"]), _p(out["R"]), int(nthreads))
     if rc != 0:
         raise ValueError(f"oracle_capon returned {rc}")
     return out

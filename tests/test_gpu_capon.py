@@ -375,3 +375,55 @@ def test_forward_backward_averaging_unsupported_beams(cap):
     P = np.zeros((2, 18), np.float32)
     e = cap.Capon().getCaponEx(z, P, None, None, x, 0.01, 16, 1, 32, 2, 20, 7, cap.opts(fb=1))
     assert e == _lib.ERR_NOT_SUPPORTED
+
+
+@pytest.mark.parametrize("Nb", [3, 5])
+def test_subspace_butler_equals_default_route(cap, Nb):
+    """The Butler matrix passed as an explicit subspace (direct products) gives
+    the sliding-DFT route's answer."""
+    from cos_gb300 import synth
+    M, L = (96, 48) if Nb == 3 else (128, 64)
+    x = synth.cube(40, 4, M, [10.0, 5.0], seed=Nb + 40)
+    B = cap.butler_matrix(Nb, L)
+    z0, P0, w0 = cap.getCaponGPU(x, 0.01, L, 1, np.zeros((Nb, L)))
+    z1, P1, w1 = cap.getCaponGPU(x, 0.01, L, 1, np.zeros((Nb, L)), subspace=B)
+    assert (np.abs(P1 - P0) / P0).max() < 2e-5
+    assert (np.abs(z1 - z0) / np.sqrt(P0)).max() < 1e-4
+
+
+@pytest.mark.parametrize("fb", [False, True])
+@pytest.mark.parametrize("bs_loading", [0, 1])
+@pytest.mark.parametrize("M,L,Nb", [(32, 16, 3), (64, 32, 5)])
+def test_general_subspace_matches_oracle(cap, M, L, Nb, bs_loading, fb):
+    """A random (non-orthonormal) subspace: element-space loading enters as
+    dl V V^H; both loadings, with and without FB averaging."""
+    from cos_gb300 import synth
+    rng = np.random.default_rng(M + Nb)
+    V = ((rng.standard_normal((Nb, L)) + 1j * rng.standard_normal((Nb, L))) / np.sqrt(2 * L)).astype(np.complex64)
+    x = synth.cube(40, 4, M, [10.0, 5.0], seed=M + 7 * Nb)
+    z, P, w = cap.getCaponGPU(x, 0.01, L, 1, None, doFBAvg=fb, loading=bs_loading, subspace=V)
+    ref = oracle.capon(x, 0.01, L, 1, Nb=Nb, V=V.astype(np.complex128), bs_loading=bool(bs_loading), fb=fb,
+                       nthreads=4)
+    assert_close(z, P, w, ref, what=f"subspace M{M} L{L} Nb{Nb} load{bs_loading} fb{int(fb)}")
+
+
+def test_general_subspace_device_frame_and_limits(cap):
+    import torch
+    from cos_gb300 import _lib, synth
+    M, L, Nb = 64, 32, 4
+    rng = np.random.default_rng(3)
+    V = ((rng.standard_normal((Nb, L)) + 1j * rng.standard_normal((Nb, L))) / np.sqrt(2 * L)).astype(np.complex64)
+    x = synth.cube(30, 3, M, [10.0], seed=9)
+    fr = cap.DeviceFrame(x=torch.from_numpy(x).cuda(), L=L, K=1, Nb=Nb, V=torch.from_numpy(V).cuda(),
+                         P=torch.empty((3, 28), device="cuda"))
+    cap.capon_frames([fr])
+    torch.cuda.synchronize()
+    ref = oracle.capon(x, 0.01, L, 1, Nb=Nb, V=V.astype(np.complex128), nthreads=3)
+    assert (np.abs(fr.P.cpu().numpy() - ref["P"]) / ref["P"]).max() < TOL_P
+    # a given subspace with Nb > 5 is outside the range-tile kernel
+    V7 = np.ones((7, L), np.complex64)
+    z = np.zeros((3, 28), np.complex64)
+    P = np.zeros((3, 28), np.float32)
+    e = _lib.lib.cos_capon_get_capon_subspace(cap._module_ctx().handle, z.ctypes.data, P.ctypes.data, None,
+                                              x.ctypes.data, V7.ctypes.data, 0.01, L, 1, M, 3, 30, 7, None)
+    assert e == _lib.ERR_NOT_SUPPORTED

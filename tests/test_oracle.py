@@ -198,3 +198,34 @@ def test_forward_backward_equals_flipped_conjugate_rows():
     r0 = oracle.capon(x, 0.0, L, K, want_R=True, fp32_scalars=False)["R"]
     r1 = oracle.capon(xt, 0.0, L, K, want_R=True, fp32_scalars=False)["R"]
     np.testing.assert_allclose(a, 0.5 * (r0 + r1), rtol=1e-12, atol=1e-12)
+
+
+def test_general_subspace_matches_numpy_restatement():
+    """Beamspace over a caller-given V against a per-pixel restatement of
+    getCaponAllC.pyx:226-231, 346-440 (element loading before the transform,
+    a = V 1, R = V R_d V^H, g_bs = V g, w_bs = R^-1 a / a^H R^-1 a,
+    z = w_bs^H g_bs); the oracle reports w = V^H w_bs-normalised weights."""
+    rng = np.random.default_rng(13)
+    M, L, K, Nb = 14, 8, 1, 3
+    x = (rng.standard_normal((2, 9, M)) + 1j * rng.standard_normal((2, 9, M))).astype(np.complex64)
+    x += (3.0 * np.exp(1j * 0.7 * np.arange(M))).astype(np.complex64)
+    V = rng.standard_normal((Nb, L)) + 1j * rng.standard_normal((Nb, L))
+    for bs_loading in (False, True):
+        o = oracle.capon(x, 0.05, L, K, Nb=Nb, V=V, bs_loading=bs_loading, fp32_scalars=False)
+        Ns, T = M - L + 1, 2 * K + 1
+        for b in range(2):
+            for p in range(9 - 2 * K):
+                d = np.array([x[b, p + t, s:s + L] for t in range(T) for s in range(Ns)]).astype(complex)
+                R = d.T @ d.conj() / (Ns * T)
+                g = np.array([x[b, p + K, l:l + Ns].astype(complex).sum() for l in range(L)]) / Ns
+                if not bs_loading:
+                    R = R + 0.05 * np.trace(R) / L * np.eye(L)
+                Rb = V @ R @ V.conj().T
+                if bs_loading:
+                    Rb = Rb + 0.05 * np.trace(Rb) / Nb * np.eye(Nb)
+                a = V @ np.ones(L)
+                Ria = np.linalg.solve(Rb, a)
+                aRia = np.vdot(a, Ria)
+                wb = Ria / aRia
+                np.testing.assert_allclose(o["z"][b, p], np.vdot(wb, V @ g), rtol=1e-9)
+                np.testing.assert_allclose(o["P"][b, p], 1.0 / aRia.real, rtol=1e-9)
