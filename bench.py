@@ -352,6 +352,12 @@ def run_gpu(args) -> None:
     except Exception as exc:
         cfg2 = {"error": str(exc)[:200]}
 
+    steering = None
+    try:
+        steering = steering_rate(stream, _peaks().get("hbm_gbs"))
+    except Exception as exc:
+        steering = {"error": str(exc)[:200]}
+
     precision = None
     if not args.no_precision and rank == 0:
         try:
@@ -400,6 +406,7 @@ def run_gpu(args) -> None:
         "adjoint": adj,
         "config2": cfg2,
         "precision": precision,
+        "steering": steering,
     }
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = {k: v for k, v in cpu_reference_rate(os.cpu_count() or 1, 16).items()
@@ -473,6 +480,47 @@ def precision_study(ctx, stream) -> dict:
     del xt
     torch.cuda.empty_cache()
     return out
+
+
+def steering_rate(stream, hbm_peak) -> dict:
+    """Time-domain steering (cos_capon_tdib) producing a config-1-sized cube
+    [Nx=256][Ny=2048][64 hydrophones] plus its delay-and-sum image, device
+    pointers; HBM roofline over the algorithmic bytes (cube and image written,
+    pixel geometry and channel data read once)."""
+    import ctypes
+    import torch
+    from cos_gb300 import _lib, capon
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import tdib_oracle  # noqa: E402
+    sc = tdib_oracle.scenario(seed=4, n_h=M, n_s=4096, n_x=NX, n_y=NY)
+    dev = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a, dtype=dt)).cuda()   # noqa: E731
+    mf = dev(sc["mfdata"], np.complex64)
+    xr, dd = dev(sc["x_r"], np.float64), dev(sc["D"], np.float64)
+    xa, ya = dev(sc["xarr"], np.float64), dev(sc["yarr"], np.float64)
+    Xd = torch.empty((NX, NY, M), dtype=torch.complex64, device="cuda")
+    img = torch.empty((NY, NX), dtype=torch.complex64, device="cuda")
+    t = sc["mtaxe"]
+    ctx = capon.Context()
+    args = (ctx.handle, mf.data_ptr(), M, t.size, float(t[0]), float(t[1] - t[0]), ctypes.c_void_p(xr.data_ptr()),
+            ctypes.c_void_p(dd.data_ptr()), sc["c"], sc["fc"], ctypes.c_void_p(xa.data_ptr()),
+            ctypes.c_void_p(ya.data_ptr()), NX, NY, Xd.data_ptr(), img.data_ptr(), 1, stream.cuda_stream)
+    for _ in range(3):
+        _lib.check(_lib.lib.cos_capon_tdib(*args), "cos_capon_tdib")
+    stream.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n = 10
+    e0.record(stream)
+    for _ in range(n):
+        _lib.lib.cos_capon_tdib(*args)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / n
+    nbytes = NX * NY * M * 8 + NX * NY * 8 + 2 * NX * NY * 8 + M * t.size * 8
+    gbs = nbytes / (ms * 1e-3) / 1e9
+    return {"workload": f"[Nx={NX}][Ny={NY}] pixels x {M} hydrophones, 4096 samples each; cube + image",
+            "ms": ms, "pixels_per_s": NX * NY / (ms * 1e-3), "bytes": nbytes,
+            "roofline_hbm": {"achieved": gbs, "peak": hbm_peak, "unit": "GB/s",
+                             "frac": gbs / hbm_peak if hbm_peak else None}}
 
 
 RTC_STAGES = ["memcpy_x_h2d", "sliding_beamspace", "build_R", "memcpy_R_d2h", "init_a", "beamspace_part1",

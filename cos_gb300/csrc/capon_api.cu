@@ -58,6 +58,7 @@ struct cos_capon_ctx {
     // stage entry points
     DevBuf A, b, sol;
     DevBuf V;           // subspace matrix of the host-pointer subspace call
+    DevBuf tdib_in;     // inputs of the host-pointer steering call
     // autotuner: chosen fused candidate per (L, K, M, w-or-R requested)
     std::map<std::tuple<int, int, int, int>, int> tuned;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -373,7 +374,7 @@ int cos_capon_destroy(cos_capon_ctx *c)
     if (!c) return COS_CAPON_ERR_INVALID_VALUE;
     cudaStreamSynchronize(c->stream);
     for (DevBuf *b : {&c->x, &c->z, &c->P, &c->w, &c->R, &c->Rwork, &c->Rlo, &c->dl, &c->Ria, &c->A, &c->b,
-                      &c->sol, &c->V})
+                      &c->sol, &c->V, &c->tdib_in})
         b->release();
     if (c->d_status) cudaFree(c->d_status);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -535,6 +536,68 @@ int cos_capon_get_capon_subspace(cos_capon_ctx *c, void *z, float *P, void *w, c
 {
     if (!V) return COS_CAPON_ERR_INVALID_VALUE;
     return get_capon_host(c, z, P, w, nullptr, x, V, d, L, Yavg, M, Nx, Nz, Nb, opts);
+}
+
+int cos_capon_tdib(cos_capon_ctx *c, const void *mfdata, int n_hydros, int n_samples, double t0, double dt,
+                   const double *x_r, const double *D, double cs, double fc, const double *xarr, const double *yarr,
+                   int n_x, int n_y, void *Xd, void *image, int on_gpu, void *stream)
+{
+    if (!c || !mfdata || !x_r || !D || !xarr || !yarr || (!Xd && !image)) return COS_CAPON_ERR_INVALID_VALUE;
+    if (n_hydros < 1 || n_samples < 2 || n_x < 1 || n_y < 1 || !(dt > 0.0) || !(cs > 0.0))
+        return COS_CAPON_ERR_LAUNCH;
+    TdibDev t;
+    memset(&t, 0, sizeof(t));
+    t.t0 = t0;
+    t.dt = dt;
+    t.inv_c = 1.0 / cs;
+    t.fc = fc;
+    t.n_hydros = n_hydros;
+    t.n_samples = n_samples;
+    t.n_x = n_x;
+    t.n_y = n_y;
+    const size_t bmf = (size_t)n_hydros * n_samples * sizeof(float2), bh = (size_t)n_hydros * sizeof(double),
+                 bg = (size_t)n_x * n_y * sizeof(double), bXd = (size_t)n_x * n_y * n_hydros * sizeof(float2),
+                 bimg = (size_t)n_x * n_y * sizeof(float2);
+    if (on_gpu) {
+        t.mf = (const float2 *)mfdata;
+        t.x_r = x_r;
+        t.D = D;
+        t.xarr = xarr;
+        t.yarr = yarr;
+        t.Xd = (float2 *)Xd;
+        t.image = (float2 *)image;
+        return launch_tdib(t, (cudaStream_t)stream);
+    }
+    // host pointers: inputs through the context's buffers, synchronous
+    int e;
+    const size_t bin = bmf + 2 * bh + 2 * bg;
+    if ((e = check_free((bin > c->tdib_in.cap ? bin : 0) + (Xd && bXd > c->x.cap ? bXd : 0) +
+                        (image && bimg > c->z.cap ? bimg : 0))))
+        return e;
+    if ((e = c->tdib_in.ensure(bin))) return e;
+    if (Xd && (e = c->x.ensure(bXd))) return e;
+    if (image && (e = c->z.ensure(bimg))) return e;
+    cudaStream_t s = c->stream;
+    unsigned char *in = (unsigned char *)c->tdib_in.p;
+    cudaError_t ce;
+    const void *src[5] = {x_r, D, xarr, yarr, mfdata};
+    const size_t len[5] = {bh, bh, bg, bg, bmf};
+    size_t off = 0;
+    for (int k = 0; k < 5; ++k) {
+        if ((ce = cudaMemcpyAsync(in + off, src[k], len[k], cudaMemcpyHostToDevice, s)) != cudaSuccess) return ce;
+        off += len[k];
+    }
+    t.x_r = (const double *)in;
+    t.D = (const double *)(in + bh);
+    t.xarr = (const double *)(in + 2 * bh);
+    t.yarr = (const double *)(in + 2 * bh + bg);
+    t.mf = (const float2 *)(in + 2 * bh + 2 * bg);
+    t.Xd = Xd ? (float2 *)c->x.p : nullptr;
+    t.image = image ? (float2 *)c->z.p : nullptr;
+    if ((e = launch_tdib(t, s))) return e;
+    if (Xd && (ce = cudaMemcpyAsync(Xd, c->x.p, bXd, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return ce;
+    if (image && (ce = cudaMemcpyAsync(image, c->z.p, bimg, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return ce;
+    return read_status(c, s, true);
 }
 
 int cos_capon_get_capon(cos_capon_ctx *c, void *z, void *w, void *R, const void *x, float d, int L, int Yavg, int M,

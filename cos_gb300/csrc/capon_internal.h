@@ -98,6 +98,19 @@ struct AdjDev {
 };
 
 int launch_adjoint(const AdjDev &a, int num_sms, cudaStream_t s);
+// time-domain steering (the step before the path)
+struct TdibDev {
+    const float2 *mf;      // [n_hydros][n_samples] matched-filtered channel data
+    const double *x_r;     // [n_hydros] receiver along-track positions
+    const double *D;       // [n_hydros] receiver depths
+    const double *xarr;    // [n_x][n_y] pixel x
+    const double *yarr;    // [n_x][n_y] pixel y
+    double t0, dt, inv_c, fc;
+    int n_hydros, n_samples, n_x, n_y;
+    float2 *Xd;            // [n_x][n_y][n_hydros] or null
+    float2 *image;         // [n_y][n_x] or null
+};
+int launch_tdib(const TdibDev &t, cudaStream_t s);
 // beamspace path (Nb > 0)
 int launch_beamspace(const FrameDev &f, float2 *R_out, cudaStream_t s);
 int launch_butler(float2 *B, int Nb, int L, cudaStream_t s);

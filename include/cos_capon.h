@@ -123,6 +123,23 @@ int cos_capon_get_capon_subspace(cos_capon_ctx *ctx, void *z, float *P, void *w,
                                  float d, int L, int Yavg, int M, int Nx, int Nz, int Nb,
                                  const cos_capon_opts *opts);
 
+/* Time-domain steering, the step that produces the Capon input cube
+ * (framework/beamformer/delay/tdibC.pyx:9-67).
+ * For beam nx, range pixel y and hydrophone n:
+ *   Xd[nx][y][n] = interp_linear(mfdata[n], tau) * exp(j 2 pi fc tau)
+ *   tau = (r_t + r_r) / c
+ * r_t and r_r are measured from the origin (mean(x_r)/2, mean(D)/2) to
+ * (xarr, yarr) and on to receiver n.  The time axis is uniform: t0 + k dt.
+ * Samples outside it are NaN, as the reference's interp1d gives.
+ * image[y][nx] = the mean of Xd over hydrophones (the reference returns
+ * image.T).  mfdata is complex64 [n_hydros][n_samples]; x_r and D are float64
+ * [n_hydros]; xarr and yarr are float64 [n_x][n_y].  Either Xd or image may be
+ * NULL.  on_gpu = 1: every pointer is device memory and the call is
+ * asynchronous on `stream`.  on_gpu = 0: host memory; synchronous. */
+int cos_capon_tdib(cos_capon_ctx *ctx, const void *mfdata, int n_hydros, int n_samples, double t0, double dt,
+                   const double *x_r, const double *D, double c, double fc, const double *xarr, const double *yarr,
+                   int n_x, int n_y, void *Xd, void *image, int on_gpu, void *stream);
+
 /* Device-pointer call: every pixel of `nframes` frames (each with its own M, L,
  * K, Nb) in one launch on `stream` (a cudaStream_t; NULL = the default stream).  Asynchronous; no host synchronisation and no allocation once the
  * context has served a call of the same or larger shape, so it can be captured
