@@ -358,6 +358,12 @@ def run_gpu(args) -> None:
     except Exception as exc:
         steering = {"error": str(exc)[:200]}
 
+    lca_line = None
+    try:
+        lca_line = lca_rate(stream, _peaks().get("hbm_gbs"))
+    except Exception as exc:
+        lca_line = {"error": str(exc)[:200]}
+
     precision = None
     if not args.no_precision and rank == 0:
         try:
@@ -407,6 +413,7 @@ def run_gpu(args) -> None:
         "config2": cfg2,
         "precision": precision,
         "steering": steering,
+        "lca": lca_line,
     }
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = {k: v for k, v in cpu_reference_rate(os.cpu_count() or 1, 16).items()
@@ -519,6 +526,41 @@ def steering_rate(stream, hbm_peak) -> dict:
     gbs = nbytes / (ms * 1e-3) / 1e9
     return {"workload": f"[Nx={NX}][Ny={NY}] pixels x {M} hydrophones, 4096 samples each; cube + image",
             "ms": ms, "pixels_per_s": NX * NY / (ms * 1e-3), "bytes": nbytes,
+            "roofline_hbm": {"achieved": gbs, "peak": hbm_peak, "unit": "GB/s",
+                             "frac": gbs / hbm_peak if hbm_peak else None}}
+
+
+def lca_rate(stream, hbm_peak) -> dict:
+    """LCA window selection (cos_capon_lca) over the config-1 pixel grid with 8
+    windows and a 5 x 1 range filter, device pointers; HBM roofline over the
+    algorithmic bytes (Z read once, the image and window index written)."""
+    import ctypes
+    import torch
+    from cos_gb300 import _lib, capon
+    Nw = 8
+    g = torch.Generator(device="cuda").manual_seed(5)
+    Z = torch.randn((NY, NX, Nw), dtype=torch.complex64, device="cuda", generator=g)
+    img = torch.empty((NY, NX), dtype=torch.complex64, device="cuda")
+    win = torch.empty((NY, NX), dtype=torch.int32, device="cuda")
+    wrf = np.ones((5, 1))
+    ctx = capon.Context()
+    args = (ctx.handle, Z.data_ptr(), NY, NX, Nw, wrf.ctypes.data, 5, 1, img.data_ptr(),
+            ctypes.c_void_p(win.data_ptr()), 1, stream.cuda_stream)
+    for _ in range(3):
+        _lib.check(_lib.lib.cos_capon_lca(*args), "cos_capon_lca")
+    stream.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n = 10
+    e0.record(stream)
+    for _ in range(n):
+        _lib.lib.cos_capon_lca(*args)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / n
+    nbytes = NY * NX * Nw * 8 + NY * NX * 12
+    gbs = nbytes / (ms * 1e-3) / 1e9
+    return {"workload": f"Z [Ny={NY}][Nx={NX}][Nw={Nw}], filter 5 x 1", "ms": ms,
+            "pixels_per_s": NX * NY / (ms * 1e-3), "bytes": nbytes,
             "roofline_hbm": {"achieved": gbs, "peak": hbm_peak, "unit": "GB/s",
                              "frac": gbs / hbm_peak if hbm_peak else None}}
 

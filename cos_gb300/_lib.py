@@ -27,7 +27,7 @@ EXPORTS = (
     "cos_capon_create", "cos_capon_destroy", "cos_capon_get_capon", "cos_capon_get_capon_ex",
     "cos_capon_run", "cos_capon_build_r", "cos_capon_solve", "cos_capon_butler",
     "cos_capon_device_status", "cos_capon_status_string", "cos_capon_run_plain_noalloc",
-    "cos_capon_backward", "cos_capon_get_capon_subspace", "cos_capon_tdib",
+    "cos_capon_backward", "cos_capon_get_capon_subspace", "cos_capon_tdib", "cos_capon_lca",
 )
 
 
@@ -78,6 +78,7 @@ def _load() -> C.CDLL:
         "cos_capon_get_capon_subspace": [vp, vp, vp, vp, vp, vp, f, i, i, i, i, i, i, C.POINTER(Opts)],
         "cos_capon_tdib": [vp, vp, i, i, C.c_double, C.c_double, vp, vp, C.c_double, C.c_double, vp, vp, i, i,
                            vp, vp, i, vp],
+        "cos_capon_lca": [vp, vp, i, i, i, vp, i, i, vp, vp, i, vp],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)

@@ -59,6 +59,7 @@ struct cos_capon_ctx {
     DevBuf A, b, sol;
     DevBuf V;           // subspace matrix of the host-pointer subspace call
     DevBuf tdib_in;     // inputs of the host-pointer steering call
+    DevBuf lca_pw;      // |Z|^2 planes of the LCA selection
     // autotuner: chosen fused candidate per (L, K, M, w-or-R requested)
     std::map<std::tuple<int, int, int, int>, int> tuned;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -374,7 +375,7 @@ int cos_capon_destroy(cos_capon_ctx *c)
     if (!c) return COS_CAPON_ERR_INVALID_VALUE;
     cudaStreamSynchronize(c->stream);
     for (DevBuf *b : {&c->x, &c->z, &c->P, &c->w, &c->R, &c->Rwork, &c->Rlo, &c->dl, &c->Ria, &c->A, &c->b,
-                      &c->sol, &c->V, &c->tdib_in})
+                      &c->sol, &c->V, &c->tdib_in, &c->lca_pw})
         b->release();
     if (c->d_status) cudaFree(c->d_status);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -597,6 +598,51 @@ int cos_capon_tdib(cos_capon_ctx *c, const void *mfdata, int n_hydros, int n_sam
     if ((e = launch_tdib(t, s))) return e;
     if (Xd && (ce = cudaMemcpyAsync(Xd, c->x.p, bXd, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return ce;
     if (image && (ce = cudaMemcpyAsync(image, c->z.p, bimg, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return ce;
+    return read_status(c, s, true);
+}
+
+int cos_capon_lca(cos_capon_ctx *c, const void *Z, int Ny, int Nx, int Nw, const double *wrf, int Yf, int Xf,
+                  void *img, int *win, int on_gpu, void *stream)
+{
+    if (!c || !Z || !wrf || !img) return COS_CAPON_ERR_INVALID_VALUE;
+    if (Ny < 1 || Nx < 1 || Nw < 1 || Yf < 1 || Xf < 1 || !(Yf & 1) || !(Xf & 1) || Yf * Xf > kLcaMaxFilter)
+        return COS_CAPON_ERR_LAUNCH;
+    LcaDev a;
+    memset(&a, 0, sizeof(a));
+    a.Ny = Ny;
+    a.Nx = Nx;
+    a.Nw = Nw;
+    a.Yf = Yf;
+    a.Xf = Xf;
+    a.Ymid = (Yf - 1) / 2;
+    a.Xmid = (Xf - 1) / 2;
+    a.single = (Yf == 1 && Xf == 1 && wrf[0] != 0.0);
+    for (int i = 0; i < Yf * Xf; ++i) a.wrf[i] = (float)wrf[i];
+    const size_t bZ = (size_t)Ny * Nx * Nw * sizeof(float2), bpw = (size_t)Ny * Nx * Nw * sizeof(float),
+                 bimg = (size_t)Ny * Nx * sizeof(float2), bwin = (size_t)Ny * Nx * sizeof(int);
+    int e;
+    if ((e = check_free((bpw > c->lca_pw.cap ? bpw : 0) +
+                        (on_gpu ? 0 : (bZ > c->x.cap ? bZ : 0) + (bimg > c->z.cap ? bimg : 0) +
+                                          (win && bwin > c->P.cap ? bwin : 0)))))
+        return e;
+    if ((e = c->lca_pw.ensure(bpw))) return e;   // |Z|^2 planes
+    if (on_gpu) {
+        a.Z = (const float2 *)Z;
+        a.img = (float2 *)img;
+        a.win = win;
+        return launch_lca(a, (float *)c->lca_pw.p, (cudaStream_t)stream);
+    }
+    if ((e = c->x.ensure(bZ)) || (e = c->z.ensure(bimg))) return e;
+    if (win && (e = c->P.ensure(bwin))) return e;
+    cudaStream_t s = c->stream;
+    cudaError_t ce;
+    if ((ce = cudaMemcpyAsync(c->x.p, Z, bZ, cudaMemcpyHostToDevice, s)) != cudaSuccess) return ce;
+    a.Z = (const float2 *)c->x.p;
+    a.img = (float2 *)c->z.p;
+    a.win = win ? (int *)c->P.p : nullptr;
+    if ((e = launch_lca(a, (float *)c->lca_pw.p, s))) return e;
+    if ((ce = cudaMemcpyAsync(img, c->z.p, bimg, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return ce;
+    if (win && (ce = cudaMemcpyAsync(win, c->P.p, bwin, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return ce;
     return read_status(c, s, true);
 }
 

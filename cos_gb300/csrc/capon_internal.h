@@ -111,6 +111,17 @@ struct TdibDev {
     float2 *image;         // [n_y][n_x] or null
 };
 int launch_tdib(const TdibDev &t, cudaStream_t s);
+// LCA window selection
+static constexpr int kLcaMaxFilter = 256;   // wrf entries
+struct LcaDev {
+    const float2 *Z;   // [Ny][Nx][Nw]
+    const float *pw;   // [Nw][Ny][Nx] |Z|^2 (filled by launch_lca)
+    float2 *img;       // [Ny][Nx]
+    int *win;          // [Ny][Nx] or null
+    int Ny, Nx, Nw, Yf, Xf, Ymid, Xmid, single;
+    float wrf[kLcaMaxFilter];
+};
+int launch_lca(const LcaDev &a, float *pw, cudaStream_t s);
 // beamspace path (Nb > 0)
 int launch_beamspace(const FrameDev &f, float2 *R_out, cudaStream_t s);
 int launch_butler(float2 *B, int Nb, int L, cudaStream_t s);

@@ -140,6 +140,18 @@ int cos_capon_tdib(cos_capon_ctx *ctx, const void *mfdata, int n_hydros, int n_s
                    const double *x_r, const double *D, double c, double fc, const double *xarr, const double *yarr,
                    int n_x, int n_y, void *Xd, void *image, int on_gpu, void *stream);
 
+/* Low-complexity adaptive (LCA) window selection (framework/beamformer/lca/
+ * lcac.py; lcacx.pyx:175-216).  Z: complex64 [Ny][Nx][Nw] beamformer outputs
+ * for Nw windows; wrf: float64 [Yf][Xf] averaging filter (odd sizes, host
+ * memory, Yf*Xf <= 256).  A 1 x 1 filter with a nonzero value selects per
+ * pixel the window of least |Z|; otherwise interior pixels take the window of
+ * least wrf-weighted sum of |Z|^2 over the neighbourhood (first minimum) and
+ * border pixels get 0 / window 0.  img: complex64 [Ny][Nx]; win: int32
+ * [Ny][Nx] or NULL.  on_gpu = 1: Z, img, win device memory, asynchronous on
+ * `stream`; 0: host memory, synchronous. */
+int cos_capon_lca(cos_capon_ctx *ctx, const void *Z, int Ny, int Nx, int Nw, const double *wrf, int Yf, int Xf,
+                  void *img, int *win, int on_gpu, void *stream);
+
 /* Device-pointer call: every pixel of `nframes` frames (each with its own M, L,
  * K, Nb) in one launch on `stream` (a cudaStream_t; NULL = the default stream).  Asynchronous; no host synchronisation and no allocation once the
  * context has served a call of the same or larger shape, so it can be captured
