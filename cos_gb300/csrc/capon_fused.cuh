@@ -243,18 +243,32 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
                 cl[rr * L + j0 + q] = lo[q];
             }
         }
-        // subarray sums of the centre rows, g[l+1] = g[l] + x[l+Ns] - x[l] (one
-        // thread per row; getCaponC.pyx:246-255 slides them the same way)
-        const float invNs = 1.0f / (float)Ns;
-        for (int q = tid; q < TILE; q += nthreads) {
-            if (q + K < rows) {
-                const float4 *xr = xe + (q + K) * XS;
-                float2 acc = make_float2(0.f, 0.f);
-                for (int s = 0; s < Ns; ++s) acc = fadd2(acc, make_float2(xr[s].x, xr[s].y));
-                for (int l = 0; l < L; ++l) {
-                    gs[q * L + l] = make_float2(acc.x * invNs, acc.y * invNs);
-                    if (l + 1 < L)
-                        acc = fadd2(acc, make_float2(xr[l + Ns].x - xr[l].x, xr[l + Ns].y - xr[l].y));
+        // subarray sums of the centre rows, g[l] = (1/Ns) sum_{s<Ns} x[s+l]
+        // (getCaponC.pyx:246-255), on all threads: item (row, 8 consecutive l)
+        // sums the first window directly and slides g[l+1] = g[l] + x[l+Ns] - x[l]
+        // over the rest
+        static_assert(L % 8 == 0 || L < 8, "subarray-sum items take 8 consecutive l");
+        {
+            constexpr int LW = L >= 8 ? 8 : L;
+            const float invNs = 1.0f / (float)Ns;
+            for (int it2 = tid; it2 < TILE * (L / LW); it2 += nthreads) {
+                const int q = it2 / (L / LW), l0 = LW * (it2 % (L / LW));
+                if (q + K < rows) {
+                    const float4 *xr = xe + (q + K) * XS;
+                    float2 a0 = make_float2(0.f, 0.f), a1 = make_float2(0.f, 0.f);
+                    int s = 0;
+                    for (; s + 1 < Ns; s += 2) {
+                        a0 = fadd2(a0, make_float2(xr[l0 + s].x, xr[l0 + s].y));
+                        a1 = fadd2(a1, make_float2(xr[l0 + s + 1].x, xr[l0 + s + 1].y));
+                    }
+                    if (s < Ns) a0 = fadd2(a0, make_float2(xr[l0 + s].x, xr[l0 + s].y));
+                    float2 acc = fadd2(a0, a1);
+#pragma unroll
+                    for (int l = l0; l < l0 + LW; ++l) {
+                        gs[q * L + l] = make_float2(acc.x * invNs, acc.y * invNs);
+                        if (l + 1 < l0 + LW)
+                            acc = fadd2(acc, make_float2(xr[l + Ns].x - xr[l].x, xr[l + Ns].y - xr[l].y));
+                    }
                 }
             }
         }
