@@ -11,7 +11,7 @@ int launch_0(const FramesParam &fp, bool wr, unsigned *st, int n, cudaStream_t s
 }
 int launch_1(const FramesParam &fp, bool wr, unsigned *st, int n, cudaStream_t s)
 {
-    return fused::launch_any<fused::Cfg<16, 8, 8, 1, 5, 32, true>>(fp, wr, st, n, s);
+    return fused::launch_any<fused::Cfg<16, 4, 8, 1, 5, 32, false>>(fp, wr, st, n, s);
 }
 int launch_2(const FramesParam &fp, bool wr, unsigned *st, int n, cudaStream_t s)
 {
@@ -20,7 +20,7 @@ int launch_2(const FramesParam &fp, bool wr, unsigned *st, int n, cudaStream_t s
 
 const FusedCandidate kCand[] = {
     {"L16.G4.W8.N1.sync.M32.T5", 16, 5, 32, launch_0},
-    {"L16.G8.W8.N1.sync.M32.T5", 16, 5, 32, launch_1},
+    {"L16.G4.W8.N1.M32.T5", 16, 5, 32, launch_1},
     {"L16.G4.W8.N1.sync.T5", 16, 5, 0, launch_2},
 };
 }  // namespace

@@ -11,7 +11,7 @@ int launch_0(const FramesParam &fp, bool wr, unsigned *st, int n, cudaStream_t s
 }
 int launch_1(const FramesParam &fp, bool wr, unsigned *st, int n, cudaStream_t s)
 {
-    return fused::launch_any<fused::Cfg<32, 16, 8, 2, 1, 64, true>>(fp, wr, st, n, s);
+    return fused::launch_any<fused::Cfg<32, 8, 8, 2, 1, 64, false>>(fp, wr, st, n, s);
 }
 int launch_2(const FramesParam &fp, bool wr, unsigned *st, int n, cudaStream_t s)
 {
@@ -20,7 +20,7 @@ int launch_2(const FramesParam &fp, bool wr, unsigned *st, int n, cudaStream_t s
 
 const FusedCandidate kCand[] = {
     {"L32.G8.W8.N2.sync.M64.T1", 32, 1, 64, launch_0},
-    {"L32.G16.W8.N2.sync.M64.T1", 32, 1, 64, launch_1},
+    {"L32.G8.W8.N2.M64.T1", 32, 1, 64, launch_1},
     {"L32.G8.W8.N2.sync.T1", 32, 1, 0, launch_2},
 };
 }  // namespace
