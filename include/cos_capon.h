@@ -93,7 +93,11 @@ typedef struct cos_capon_ctx cos_capon_ctx;
 /* Create / destroy a context.  The context owns the device buffers of the
  * host-pointer calls (grown on demand, freed by destroy), its stream and its
  * device status word -- the role of the reference's Capon object
- * (Capon.h:13-125, Capon.cpp:50-71).  Uses the calling thread's current device. */
+ * (Capon.h:13-125, Capon.cpp:50-71).  Uses the calling thread's current device.
+ * Like that object, a context is not thread-safe: its work buffers (the
+ * materialised-R pipelines, the LCA planes, the staging of host calls) serve
+ * one call at a time, so calls that may overlap -- from several threads, or
+ * device calls on different streams -- need a context each. */
 int cos_capon_create(cos_capon_ctx **ctx);
 int cos_capon_destroy(cos_capon_ctx *ctx);
 
@@ -153,7 +157,8 @@ int cos_capon_lca(cos_capon_ctx *ctx, const void *Z, int Ny, int Nx, int Nw, con
                   void *img, int *win, int on_gpu, void *stream);
 
 /* Device-pointer call: every pixel of `nframes` frames (each with its own M, L,
- * K, Nb) in one launch on `stream` (a cudaStream_t; NULL = the default stream).  Asynchronous; no host synchronisation and no allocation once the
+ * K, Nb) in one call on `stream` (fused frames of equal L, K, M share one
+ * persistent launch) (a cudaStream_t; NULL = the default stream).  Asynchronous; no host synchronisation and no allocation once the
  * context has served a call of the same or larger shape, so it can be captured
  * into a CUDA graph after one warm-up call. */
 int cos_capon_run(cos_capon_ctx *ctx, const cos_capon_frame *frames, int nframes,
@@ -203,7 +208,10 @@ typedef struct cos_capon_adjoint {
 int cos_capon_backward(cos_capon_ctx *ctx, const cos_capon_adjoint *adj, void *stream);  /* NULL = default stream */
 
 /* Status word of the last launch on this context (0, or COS_CAPON_ERR_TIMEOUT
- * when a bounded device-side wait gave up).  Synchronises the context stream. */
+ * when a bounded device-side wait gave up).  Synchronises the context stream.
+ * A non-positive Cholesky pivot (e.g. no loading on a rank-deficient R) is not
+ * an error, as in the reference, whose solver reports none: the affected
+ * pixels' outputs are not finite. */
 int cos_capon_device_status(cos_capon_ctx *ctx);
 
 /* No counterpart in the reference.  Allocation-free variant of the plain FP32

@@ -4,6 +4,7 @@ import ctypes as C
 import os
 import re
 
+import numpy as np
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -72,3 +73,28 @@ def test_cxx_shim_compiles():
         p = subprocess.run(["g++", "-std=c++11", "-fsyntax-only", "-I", os.path.join(ROOT, "include"), f],
                            capture_output=True, text=True)
         assert p.returncode == 0, p.stderr
+
+
+def test_new_entry_points_reject_null_context_without_touching_the_gpu():
+    """The steering, LCA and subspace calls validate their arguments first."""
+    import ctypes as C
+    from cos_gb300 import _lib
+    x = np.zeros(8, np.complex64)
+    d = np.zeros(8)
+    assert _lib.lib.cos_capon_tdib(None, x.ctypes.data, 2, 4, 0.0, 1.0, d.ctypes.data, d.ctypes.data, 1500.0,
+                                   1e5, d.ctypes.data, d.ctypes.data, 2, 2, x.ctypes.data, None, 0,
+                                   None) == _lib.ERR_INVALID_VALUE
+    assert _lib.lib.cos_capon_lca(None, x.ctypes.data, 2, 2, 2, d.ctypes.data, 1, 1, x.ctypes.data, None, 0,
+                                  None) == _lib.ERR_INVALID_VALUE
+    assert _lib.lib.cos_capon_get_capon_subspace(None, x.ctypes.data, None, None, x.ctypes.data, x.ctypes.data,
+                                                 0.01, 4, 1, 8, 1, 4, 2, None) == _lib.ERR_INVALID_VALUE
+
+
+def test_steering_time_axis_must_be_uniform():
+    import pytest
+    from cos_gb300 import tdib
+    assert tdib._axis(np.arange(10) * 0.5 + 2.0) == (2.0, 0.5)
+    with pytest.raises(ValueError):
+        tdib._axis(np.array([0.0, 1.0, 3.0]))
+    with pytest.raises(ValueError):
+        tdib._axis(np.array([1.0]))
