@@ -211,14 +211,10 @@ def run_gpu(args) -> None:
     import torch
     from cos_gb300 import _lib, capon, synth
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    from cos_gb300 import replicas
+    rank, local, world = replicas.env()
     torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
+    dist = replicas.init("nccl")
 
     x_host = synth.config1(seed=1 + rank)["x"]
     xt = torch.from_numpy(x_host).cuda()
@@ -239,8 +235,7 @@ def run_gpu(args) -> None:
             for _ in range(warmup):
                 capon.capon_frames([f], ctx, o, stream)
         stream.synchronize()
-        if dist:
-            dist.barrier()
+        replicas.barrier(dist)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         with torch.cuda.stream(stream):
@@ -250,18 +245,14 @@ def run_gpu(args) -> None:
             e1.record(stream)
         e1.synchronize()
         torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1) / steps
-        if dist:
-            t = torch.tensor([ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = replicas.max_over_ranks(dist, e0.elapsed_time(e1) / steps, device="cuda")
         return ms, f
 
     # fused (headline), with clocks sampled during the timed region
     with Clocks(local) as clk:
         ms, f = time_form(_lib.FORM_FUSED, args.steps, args.warmup)
     clocks = clk.summary()
-    value = NPIX * world / (ms * 1e-3)
+    value = replicas.aggregate_rate(NPIX, ms, world)
 
     # plain FP32 three-stage form (denominator), fewer steps
     ms_plain, _ = time_form(_lib.FORM_PLAIN, max(2, min(args.steps, 5)), max(1, min(args.warmup, 2)))
@@ -274,16 +265,11 @@ def run_gpu(args) -> None:
     xn, zn, Pn = xp.numpy(), zp.numpy(), Pp.numpy()
     for _ in range(max(1, args.warmup)):
         _lib.check(cctx.getCaponEx(zn, Pn, None, None, xn, D, L, K, M, NX, NY, 0))
-    if dist:
-        dist.barrier()
+    replicas.barrier(dist)
     t0 = time.perf_counter()
     for _ in range(args.steps):
         _lib.check(cctx.getCaponEx(zn, Pn, None, None, xn, D, L, K, M, NX, NY, 0))
-    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
-    if dist:
-        t = torch.tensor([e2e_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = replicas.max_over_ranks(dist, (time.perf_counter() - t0) * 1e3 / args.steps, device="cuda")
 
     # adjoint cost: forward with the weights saved (absolute loading, as the
     # differentiable path runs it) and the adjoint kernel over the full frame
@@ -420,8 +406,7 @@ def run_gpu(args) -> None:
                                 if k != "seconds"}
     if rank == 0:
         print(json.dumps(line))
-    if dist:
-        dist.destroy_process_group()
+    replicas.finalize(dist)
 
 
 PRECISION_FORMS = [  # name, form, refine
