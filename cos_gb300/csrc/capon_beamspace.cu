@@ -286,7 +286,7 @@ struct BsTileSmem {
 };
 
 template <int NB>
-__global__ void __launch_bounds__(kTileThreads)
+__global__ void __launch_bounds__(kTileThreads, 2)
 beamspace_tile_kernel(FrameDev f, float2 *__restrict__ Rbs, int tile)
 {
     constexpr int NQ = BsTile<NB>::NQ;

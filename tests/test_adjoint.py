@@ -80,3 +80,80 @@ def test_cuda_adjoint_matches_reference_gradient(L, K, M, Ny):
     gt_err = (torch.abs(tg.grad.cpu().double() - tr.grad).max() / torch.abs(tr.grad).max()).item()
     print(f"L{L}: P {relP:.2e} grad x {gx_err:.2e} delta {gd_err:.2e} tau {gt_err:.2e}")
     assert gx_err < 1e-3 and gd_err < 1e-3 and gt_err < 1e-3
+
+
+def _pixel_losses(x, delta, tau, L, K, f0, b, p):
+    """FP64 output power of the listed (beam, pixel) pairs (torch.linalg)."""
+    return capon_power_reference(x, delta, tau, L, K, f0, pixels=(b, p))
+
+
+@pytest.mark.gpu
+def test_config4_gradients_full_frame():
+    """The differentiation workload as specified: the config-1 batch
+    [Nx=256][Ny=2048][M=64], L=32, K=2, delays tau_m ~ U(-0.05, 0.05) applied as
+    exp(-j 2 pi f0 tau_m) with f0 = 0.25, a learnable absolute loading delta
+    initialised at 0.01 tr(R)/L, loss = sum of P over a seeded 64 x 64 pixel
+    mask.  The CUDA gradients are checked against FP64 central differences
+    (step 1e-6) for 256 random input samples inside the mask's support, and
+    against torch.linalg autograd for delta and tau."""
+    from cos_gb300 import synth
+    from cos_gb300.autograd import capon_power
+    L, K, f0 = 32, 2, 0.25
+    c = synth.config1(seed=4)
+    x = c["x"]
+    Nx, Ny, M = x.shape
+    rng = np.random.default_rng(4)
+    tau0 = rng.uniform(-0.05, 0.05, M)
+    # 0.01 tr(R)/L of the normalised covariance = 0.01 * mean snapshot energy per element
+    delta0 = 0.01 * float(np.mean(np.abs(x.astype(np.complex128)) ** 2))
+    b0, p0 = int(rng.integers(0, Nx - 64)), int(rng.integers(0, Ny - 2 * K - 64))
+    mask = np.zeros((Nx, Ny - 2 * K))
+    mask[b0:b0 + 64, p0:p0 + 64] = 1.0
+
+    xg = torch.from_numpy(x).cuda().requires_grad_(True)
+    dg = torch.tensor(delta0, dtype=torch.float32, device="cuda", requires_grad=True)
+    tg = torch.tensor(tau0, dtype=torch.float32, device="cuda", requires_grad=True)
+    Pg = capon_power(xg, dg, tg, L, K, f0)
+    (Pg * torch.from_numpy(mask).float().cuda()).sum().backward()
+    gx = xg.grad.cpu().numpy()
+
+    # torch.linalg reference over the mask (FP64)
+    bb, pp = np.nonzero(mask)
+    bt, pt = torch.from_numpy(bb), torch.from_numpy(pp)
+    x64 = torch.from_numpy(x.astype(np.complex128))
+    dr = torch.tensor(delta0, dtype=torch.float64, requires_grad=True)
+    tr = torch.tensor(tau0, requires_grad=True)
+    _pixel_losses(x64, dr, tr, L, K, f0, bt, pt).sum().backward()
+    gd_err = abs(dg.grad.item() - dr.grad.item()) / abs(dr.grad.item())
+    gt_err = (torch.abs(tg.grad.cpu().double() - tr.grad).max() / torch.abs(tr.grad).max()).item()
+
+    # FP64 central differences for 256 random input samples under the mask
+    h = 1e-6
+    errs = []
+    scale = np.abs(gx[b0:b0 + 64, p0:p0 + 64 + 2 * K]).max()
+    for _ in range(256):
+        b = b0 + int(rng.integers(0, 64))
+        y = p0 + int(rng.integers(0, 64 + 2 * K))
+        m = int(rng.integers(0, M))
+        unit = 1.0 if rng.random() < 0.5 else 1j
+        # pixels of beam b whose window contains row y and lie in the mask
+        ps = np.arange(max(p0, y - 2 * K), min(p0 + 64, y + 1))
+        if ps.size == 0:
+            continue
+        # only beam b's rows ps[0] .. ps[-1] + 2K enter these pixels
+        r0 = int(ps[0])
+        sub = x64[b:b + 1, r0:int(ps[-1]) + 2 * K + 1]
+        bsel, psel = torch.zeros(ps.size, dtype=torch.long), torch.from_numpy(ps - r0)
+        xp, xm = sub.clone(), sub.clone()
+        xp[0, y - r0, m] += h * unit
+        xm[0, y - r0, m] -= h * unit
+        with torch.no_grad():
+            fd = (_pixel_losses(xp, dr, tr, L, K, f0, bsel, psel).sum() -
+                  _pixel_losses(xm, dr, tr, L, K, f0, bsel, psel).sum()).item() / (2 * h)
+        g = gx[b, y, m]
+        expect = g.real if unit == 1.0 else g.imag
+        errs.append(abs(fd - expect) / scale)
+    print(f"config 4: delta {gd_err:.2e} tau {gt_err:.2e} x (FD, {len(errs)} samples, max rel to scale) "
+          f"{max(errs):.2e}")
+    assert len(errs) >= 200
+    assert gd_err < 1e-3 and gt_err < 1e-3 and max(errs) < 1e-3
