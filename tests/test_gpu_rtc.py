@@ -85,3 +85,29 @@ def test_error_codes_match_reference_gpu_library(rtc):
             assert e == ours == 719, (Nx, Nb, e, ours)
     finally:
         os.chdir(cwd)
+
+
+@pytest.mark.parametrize("M,L,Nb", [(32, 16, 3), (64, 32, 5)])
+def test_beamspace_against_reference_gpu_library(rtc, M, L, Nb):
+    """The reference's default beamspace route (Butler matrix, three batched
+    cuBLAS GEMMs around an Nb x Nb solve, Capon.cpp:285-417) on the same cube:
+    both are held against the FP64 oracle, this build to the fused tolerance,
+    and the two agree to within the reference's own FP32 error."""
+    import oracle
+    from cos_gb300 import capon, synth
+    K = 1
+    x = synth.cube(40, 4, M, [10.0, 5.0], seed=M + Nb)
+    e, z_r, w_r, _ = _run_rtc(rtc, x, 0.01, L, K, Nb)
+    assert e == 0
+    z, R, w, e2 = capon.getCaponCUDAPy(x, 0.01, L, K, np.zeros((Nb, L)), want_R=False)
+    assert e2 == 0
+    ref = oracle.capon(x, 0.01, L, K, Nb=Nb, nthreads=4)
+    sP = np.sqrt(ref["P"])
+    ez_ours = (np.abs(z - ref["z"]) / sP).max()
+    ez_rtc = (np.abs(z_r - ref["z"]) / sP).max()
+    ew_ours = (np.linalg.norm(w - ref["w"], axis=-1) / np.linalg.norm(ref["w"], axis=-1)).max()
+    ew_rtc = (np.linalg.norm(w_r - ref["w"], axis=-1) / np.linalg.norm(ref["w"], axis=-1)).max()
+    print(f"M{M} L{L} Nb{Nb}: z ours {ez_ours:.2e} ref-lib {ez_rtc:.2e}; w ours {ew_ours:.2e} ref-lib {ew_rtc:.2e}")
+    assert ez_ours < 1e-3 and ew_ours < 2e-3
+    assert ez_rtc < 1e-2 and ew_rtc < 5e-2
+    assert (np.abs(z - z_r) / sP).max() < 2 * ez_rtc + 1e-3
