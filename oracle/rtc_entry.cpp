@@ -24,3 +24,24 @@ extern "C" void rtc_release(void)
     delete g_capon;
     g_capon = nullptr;
 }
+
+#include "BuildR.h"
+#include "Solver.h"
+
+// ISolver::solve (Solver.cpp:23-116): batched general systems, host pointers
+extern "C" int rtc_solve(void *x, void *A, void *b, int N, int batch)
+{
+    Solver s;
+    Complex<float> *xp = (Complex<float> *)x, *Ap = (Complex<float> *)A, *bp = (Complex<float> *)b;
+    bool xg = false, Ag = false, bg = false;
+    return s.solve(xp, Ap, bp, N, batch, xg, Ag, bg);
+}
+
+// IBuildR::getR (BuildR.cpp:21-106): covariance per pixel, host pointers
+extern "C" int rtc_build_r(void *R, void *x, float d, int L, int Yavg, int M, int Nx, int Nz, int Nb)
+{
+    BuildR br;
+    Complex<float> *Rp = (Complex<float> *)R, *xp = (Complex<float> *)x;
+    bool Rg = false, xg = false;
+    return br.getR(Rp, xp, d, L, Yavg, M, Nx, Nz, Nb, Rg, xg);
+}
