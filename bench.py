@@ -271,6 +271,18 @@ def run_gpu(args) -> None:
         _lib.check(cctx.getCaponEx(zn, Pn, None, None, xn, D, L, K, M, NX, NY, 0))
     e2e_ms = replicas.max_over_ranks(dist, (time.perf_counter() - t0) * 1e3 / args.steps, device="cuda")
 
+    # the reference-facing drop-in call (Capon::getCapon semantics: z and w, no
+    # P), end to end from pinned host buffers
+    wp = torch.empty((NX, npy, L), dtype=torch.complex64).pin_memory()
+    wn = wp.numpy()
+    for _ in range(max(1, args.warmup)):
+        _lib.check(cctx.getCapon(zn, wn, None, xn, D, L, K, M, NX, NY, 0))
+    replicas.barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        _lib.check(cctx.getCapon(zn, wn, None, xn, D, L, K, M, NX, NY, 0))
+    dropin_ms = replicas.max_over_ranks(dist, (time.perf_counter() - t0) * 1e3 / args.steps, device="cuda")
+
     # adjoint cost: forward with the weights saved (absolute loading, as the
     # differentiable path runs it) and the adjoint kernel over the full frame
     adj = None
@@ -383,6 +395,10 @@ def run_gpu(args) -> None:
                    "sample": "beams 0,128,255 vs FP64 oracle"},
         "e2e": {"value": NPIX * world / (e2e_ms * 1e-3), "unit": "pixels/s", "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": int(x_host.nbytes), "d2h_bytes_per_step": int(zn.nbytes + Pn.nbytes)},
+        "e2e_getcapon_zw": {"value": replicas.aggregate_rate(NPIX, dropin_ms, world), "unit": "pixels/s",
+                            "ms_per_step": dropin_ms, "h2d_bytes_per_step": int(x_host.nbytes),
+                            "d2h_bytes_per_step": int(zn.nbytes + wn.nbytes),
+                            "call": "cos_capon_get_capon (Capon::getCapon drop-in: z and w)"},
         "gpu_launches": args.steps,
         "roofline": {"bound": "fp32", "achieved": achieved_tf, "peak": fp32, "unit": "TFLOP/s",
                      "frac": achieved_tf / fp32, "traffic": TRAFFIC_PER_PIXEL * NPIX, "traffic_unit": "bytes",
