@@ -38,8 +38,11 @@ namespace tc {
 
 static constexpr int kThreads = 256;   // eight warps, two per 32-lane TMEM quadrant
 static constexpr int kMaxTracePartials = 256;  // P * nseg <= kThreads
-static constexpr int kTmemCols = 512;  // the whole TMEM of the SM (one CTA per SM)
-static constexpr int kMinSmem = 116 * 1024;  // forces one resident CTA per SM
+static constexpr int kTmemCols = 256;  // half the SM's TMEM: two CTAs share an SM
+// shared-memory floor so that no third CTA lands on an SM (it would wait in
+// tcgen05.alloc for a CTA to finish), and the ceiling under which two fit
+static constexpr int kMinSmem = 77 * 1024;
+static constexpr int kTwoCtaSmem = 113 * 1024;
 
 struct Geom {
     int P;          // pixels per slot (128 / M)
@@ -53,7 +56,10 @@ struct Geom {
     int aBytes;     // one copy of A of one slot
     int bBytes;     // one copy of B of one slot
     int slotBytes;  // all copies of A and B of one slot
-    int opBytes;    // S slots
+    int opBytes;    // S slots (the band and the staged R reuse this area after the MMAs)
+    int xsOff;      // staged windows: S*P pixels x T rows x M samples
+    int bandOff;    // offset of the band (inside the operand area)
+    int rstOff;     // offset of the staged R (inside the operand area)
     int bs;         // band row stride in floats (even, L+2)
     int nseg;       // segments per diagonal in the smoothing (P*L*nseg <= threads)
     int smem;
@@ -180,7 +186,7 @@ COS_DEV int core_off(int r, int kc, int sbo) { return (r >> 3) * sbo + kc * 128 
 // Eight warps: warps w and w+4 share TMEM lane quadrant w%4 and split its
 // columns on readout.
 template <int SPLIT>
-__global__ void __launch_bounds__(kThreads, 1) tc_cov_kernel(const __grid_constant__ Params prm)
+__global__ void __launch_bounds__(kThreads, 2) tc_cov_kernel(const __grid_constant__ Params prm)
 {
     constexpr bool BF16 = SPLIT == COS_CAPON_FORM_TC_BF16X3;
     constexpr int NT = SPLIT == COS_CAPON_FORM_TC_TF32 ? 1 : 3;   // products per slot
@@ -190,13 +196,14 @@ __global__ void __launch_bounds__(kThreads, 1) tc_cov_kernel(const __grid_consta
     const int M = f.M, L = f.L, T = 2 * f.K + 1, Ns = M - L + 1, twoT = 2 * T;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     unsigned char *ops = smem;                                       // S slots of operands
-    float *bandRe = (float *)(smem + g.opBytes);                     // [128][bs]
+    float *bandRe = (float *)(smem + g.bandOff);                     // [128][bs], after the MMAs
     float *bandIm = bandRe + 128 * g.bs;                             // [128][bs]
-    float *trp = bandIm + 128 * g.bs;                                // [P][nseg] trace partials
+    float2 *Rst = (float2 *)(smem + g.rstOff);                       // staged R of one slot
+    float2 *xs = (float2 *)(smem + g.xsOff);                         // staged pixel windows
+    float *trp = (float *)(smem + g.xsOff + (size_t)g.S * g.P * T * M * sizeof(float2));
     uint64_t *bar = (uint64_t *)(trp + kMaxTracePartials);
     uint32_t *tmem_slot = (uint32_t *)(bar + 1);
     int *flag = (int *)(tmem_slot + 1);
-    float2 *Rst = (float2 *)ops;                                      // staged R of one slot
 
     const long long npix = (long long)f.Nx * f.Npy;
     const long long per_pass = (long long)g.S * g.P;
@@ -221,6 +228,22 @@ __global__ void __launch_bounds__(kThreads, 1) tc_cov_kernel(const __grid_consta
 
     for (long long u = blockIdx.x; u < units; u += gridDim.x) {
         const long long pix0 = u * per_pass;
+        // 0. stage the unit's pixel windows (T rows each) in shared memory
+        {
+            const int npx = g.S * g.P;
+            const int per = T * M;
+            for (int i = tid; i < npx * per; i += kThreads) {
+                const int q = i / per, off = i % per;
+                const long long pix = pix0 + q;
+                float2 v = make_float2(0.f, 0.f);
+                if (pix < npix) {
+                    const int bx = (int)(pix / f.Npy), py = (int)(pix % f.Npy);
+                    v = f.x[((size_t)bx * f.Ny + py) * M + off];
+                }
+                xs[i] = v;
+            }
+        }
+        __syncthreads();
         // 1. operands: A and B of every slot, hi (and lo) copies.  For a fixed
         // (slot, K chunk) the (pixel, window row) of each element pair is the
         // same for every operand row, so it is resolved once per chunk.
@@ -237,8 +260,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_cov_kernel(const __grid_consta
                     const int pk = k / twoT, t = (k % twoT) >> 1;
                     const long long pix = pix0 + (long long)s * g.P + pk;
                     if (pk < g.P && pix < npix) {
-                        const int bx = (int)(pix / f.Npy), py = (int)(pix % f.Npy);
-                        rowp[e] = f.x + ((size_t)bx * f.Ny + py + t) * M;
+                        rowp[e] = xs + ((size_t)(s * g.P + pk) * T + t) * M;
                         pkv[e] = pk;
                     }
                 }
@@ -261,7 +283,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_cov_kernel(const __grid_consta
                 for (int e = 0; e < 4; ++e) {
                     float2 v = make_float2(0.f, 0.f);
                     if (rowp[e] && part != 3 && (part != 0 || pkv[e] == p)) {
-                        v = __ldg(rowp[e] + ch);
+                        v = rowp[e][ch];
                         if (part == 2) v = make_float2(-v.y, v.x);
                     }
                     split<SPLIT>(v.x, hi[2 * e], lo[2 * e]);
@@ -411,18 +433,27 @@ static bool tc_geometry(const FrameDev &f, int split, Geom &g)
     g.bBytes = g.N * g.Ktot * g.esize;
     g.slotBytes = g.copies * (g.aBytes + g.bBytes);
     g.bs = L + 2;   // odd float offset between rows' writes of one band column
-    const int bandBytes = 2 * 128 * g.bs * (int)sizeof(float) + kMaxTracePartials * (int)sizeof(float);
-    const int tail = 64;
+    const int bandBytes = 2 * 128 * g.bs * (int)sizeof(float);
+    const int tail = kMaxTracePartials * (int)sizeof(float) + 64;
     g.nseg = kThreads / (g.P * L);
     if (g.nseg > L) g.nseg = L;
     const int rstBytes = g.P * L * L * (int)sizeof(float2);
-    g.S = kTmemCols / g.N;
-    if (g.S > 4) g.S = 4;
-    while (g.S > 1 && g.S * g.slotBytes + bandBytes + tail > 227 * 1024) --g.S;
-    g.opBytes = g.S * g.slotBytes;
-    if (g.opBytes < rstBytes) g.opBytes = rstBytes;
-    g.opBytes = (g.opBytes + 1023) & ~1023;
-    g.smem = g.opBytes + bandBytes + tail;
+    const int winBytes = g.P * T * M * (int)sizeof(float2);   // per slot
+    auto layout = [&](int S) {
+        g.S = S;
+        int area = S * g.slotBytes;
+        const int after = ((bandBytes + 15) & ~15) + rstBytes;   // band, then staged R
+        if (area < after) area = after;
+        g.opBytes = (area + 1023) & ~1023;
+        g.bandOff = 0;
+        g.rstOff = (bandBytes + 15) & ~15;
+        g.xsOff = g.opBytes;
+        g.smem = g.opBytes + S * winBytes + tail;
+    };
+    int S = kTmemCols / g.N;
+    if (S > 4) S = 4;
+    layout(S);
+    while (g.S > 1 && g.smem > kTwoCtaSmem) layout(g.S - 1);
     if (g.smem > 227 * 1024) return false;
     if (g.smem < kMinSmem) g.smem = kMinSmem;
     // instruction descriptor: FP32 accumulator, K-major A and B, N>>3, M>>4
@@ -445,7 +476,9 @@ static int launch_split(const Params &p, int num_sms, cudaStream_t s)
     if (e != cudaSuccess) return e;
     const long long npix = (long long)p.f.Nx * p.f.Npy;
     const long long units = (npix + (long long)p.g.S * p.g.P - 1) / ((long long)p.g.S * p.g.P);
-    const int grid = (int)(units < num_sms ? units : num_sms);
+    const long long per_sm = p.g.smem <= kTwoCtaSmem ? 2 : 1;
+    const long long cap = per_sm * num_sms;
+    const int grid = (int)(units < cap ? units : cap);
     tc_cov_kernel<SPLIT><<<grid, kThreads, p.g.smem, s>>>(p);
     return cudaGetLastError();
 }
