@@ -362,6 +362,13 @@ def run_gpu(args) -> None:
     except Exception as exc:
         lca_line = {"error": str(exc)[:200]}
 
+    sliding = None
+    if not args.no_precision and rank == 0:
+        try:
+            sliding = sliding_inverse_study(ctx, stream, xt, x_host)
+        except Exception as exc:
+            sliding = {"error": str(exc)[:200]}
+
     precision = None
     if not args.no_precision and rank == 0:
         try:
@@ -416,6 +423,7 @@ def run_gpu(args) -> None:
         "precision": precision,
         "steering": steering,
         "lca": lca_line,
+        "sliding_inverse": sliding,
     }
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = {k: v for k, v in cpu_reference_rate(os.cpu_count() or 1, 16).items()
@@ -423,6 +431,51 @@ def run_gpu(args) -> None:
     if rank == 0:
         print(json.dumps(line))
     replicas.finalize(dist)
+
+
+SLIDING_D = 0.5          # absolute loading on the normalised covariance
+SLIDING_SEGMENTS = (4, 8, 32)
+
+
+def sliding_inverse_study(ctx, stream, xt, x_host) -> dict:
+    """The config-1 frame through FORM_SLIDING_INVERSE (R_d^-1 carried along
+    range by Sherman-Morrison changes) at a few build-up intervals, beside the
+    fused kernel at the same absolute loading; P errors on sampled beams
+    against the FP64 direct solve."""
+    import torch
+    from cos_gb300 import _lib, capon
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle  # noqa: E402
+    npy = NY - 2 * K
+    beams = [0, 128, 255]
+    ref = oracle.capon(np.ascontiguousarray(x_host[beams]), SLIDING_D, L, K, want_w=False, nthreads=3,
+                       absolute=True, fp32_scalars=False)
+
+    def run(o, steps=3):
+        f = capon.DeviceFrame(x=xt, L=L, K=K, d=SLIDING_D,
+                              z=torch.empty((NX, npy), dtype=torch.complex64, device="cuda"),
+                              P=torch.empty((NX, npy), dtype=torch.float32, device="cuda"))
+        with torch.cuda.stream(stream):
+            capon.capon_frames([f], ctx, o, stream)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(steps):
+                capon.capon_frames([f], ctx, o, stream)
+            e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        P = f.P.cpu().numpy()[beams]
+        e = np.abs(P - ref["P"]) / ref["P"]
+        return {"ms": ms, "pixels_per_s": NPIX / (ms * 1e-3), "P_rel_err_max": float(np.nanmax(e)),
+                "P_rel_err_median": float(np.nanmedian(e)), "nonfinite": int(np.sum(~np.isfinite(P)))}
+
+    out = {"workload": f"config-1 frame, absolute loading {SLIDING_D} on the normalised R",
+           "fused_same_loading": run(capon.opts(form=_lib.FORM_FUSED, loading=_lib.LOAD_ABSOLUTE))}
+    for seg in SLIDING_SEGMENTS:
+        out[f"segment_{seg}"] = run(capon.opts(form=_lib.FORM_SLIDING_INVERSE, loading=_lib.LOAD_ABSOLUTE,
+                                               segment=seg))
+    out["error_sample"] = "beams 0,128,255 vs the FP64 direct solve (oracle, absolute loading)"
+    return out
 
 
 PRECISION_FORMS = [  # name, form, refine

@@ -19,6 +19,7 @@ ERR_NOT_SUPPORTED = 801
 ERR_TIMEOUT = 909
 
 FORM_FUSED, FORM_PLAIN, FORM_TC_TF32, FORM_TC_BF16X3, FORM_TC_TF32X3 = 0, 1, 2, 3, 4
+FORM_SLIDING_INVERSE = 5
 LOAD_ELEMENT, LOAD_BEAMSPACE, LOAD_ABSOLUTE = 0, 1, 2
 R_REFERENCE, R_NORMALISED = 0, 1
 
@@ -33,7 +34,7 @@ EXPORTS = (
 
 class Opts(C.Structure):
     _fields_ = [("form", C.c_int), ("loading", C.c_int), ("r_layout", C.c_int), ("refine", C.c_int),
-                ("fb", C.c_int)]
+                ("fb", C.c_int), ("segment", C.c_int)]
 
 
 class Frame(C.Structure):

@@ -67,7 +67,8 @@ struct cos_capon_ctx {
     cudaStream_t stream2 = nullptr;
 };
 
-static const cos_capon_opts kDefaultOpts = {COS_CAPON_FORM_FUSED, COS_CAPON_LOAD_ELEMENT, COS_CAPON_R_REFERENCE, 0, 0};
+static const cos_capon_opts kDefaultOpts = {COS_CAPON_FORM_FUSED, COS_CAPON_LOAD_ELEMENT, COS_CAPON_R_REFERENCE, 0, 0,
+                                            0};
 
 // Argument checks of Capon::getCapon (Capon.cpp:98-107) and BuildR::getR
 // (BuildR.cpp:37-48), plus this build's own limits.
@@ -115,6 +116,7 @@ static FrameDev make_frame(const cos_capon_frame &fr, const cos_capon_opts &o)
     f.r_layout = o.r_layout;
     f.refine = o.refine;
     f.fb = o.fb ? 1 : 0;
+    if (o.form == COS_CAPON_FORM_SLIDING_INVERSE) f.tile = o.segment;
     return f;
 }
 
@@ -273,7 +275,21 @@ static int run_tc(cos_capon_ctx *c, FrameDev f, int split, bool refine, cudaStre
 
 static int run_frames(cos_capon_ctx *c, const FrameDev *fs, int n, const cos_capon_opts &o, cudaStream_t s)
 {
-    if (o.form < COS_CAPON_FORM_FUSED || o.form > COS_CAPON_FORM_TC_TF32X3) return COS_CAPON_ERR_NOT_SUPPORTED;
+    if (o.form < COS_CAPON_FORM_FUSED || o.form > COS_CAPON_FORM_SLIDING_INVERSE) return COS_CAPON_ERR_NOT_SUPPORTED;
+    if (o.form == COS_CAPON_FORM_SLIDING_INVERSE) {
+        // every frame is checked before the first launch
+        for (int k = 0; k < n; ++k) {
+            const FrameDev &f = fs[k];
+            if (f.Nb != 0 || f.fb || f.R || f.refine || f.loading != COS_CAPON_LOAD_ABSOLUTE || f.L > 32)
+                return COS_CAPON_ERR_NOT_SUPPORTED;
+            if (!(f.d > 0.f) || f.tile < 0) return COS_CAPON_ERR_LAUNCH;
+        }
+        for (int k = 0; k < n; ++k) {
+            int e = launch_sliding_inverse(fs[k], c->d_status, s);
+            if (e) return e;
+        }
+        return 0;
+    }
     if (is_tc_form(o.form))
         for (int k = 0; k < n; ++k)
             if (fs[k].Nb != 0 || !tc_supported(fs[k], o.form)) return COS_CAPON_ERR_NOT_SUPPORTED;
@@ -432,7 +448,8 @@ static int get_capon_host(cos_capon_ctx *c, void *z, float *P, void *w, void *R,
     need += (P && bp > c->P.cap) ? bp : 0;
     need += (w && bw > c->w.cap) ? bw : 0;
     need += (R && bR > c->R.cap) ? bR : 0;
-    if (plain && Nb == 0) {
+    const bool sliding = o.form == COS_CAPON_FORM_SLIDING_INVERSE;
+    if (plain && Nb == 0 && !sliding) {
         need += (bR > c->Rwork.cap ? bR : 0) + (bw > c->Ria.cap ? bw : 0);
         if (!(o.form == COS_CAPON_FORM_PLAIN && !o.refine)) need += bR > c->Rlo.cap ? bR : 0;
     }
@@ -456,7 +473,7 @@ static int get_capon_host(cos_capon_ctx *c, void *z, float *P, void *w, void *R,
     // chunk overlap the kernel of the other.  The first call of a fused shape
     // runs whole, so the autotuner times the frame once, on one stream.
     const bool fused = use_fused(make_frame(probe, o), o);
-    const bool no_scratch = fused || Nb > 0;
+    const bool no_scratch = fused || Nb > 0 || sliding;
     const bool tuned = !fused || c->tuned.count(std::make_tuple(L, Yavg, M, (int)(w != nullptr || R != nullptr)));
     if (no_scratch && tuned && !R && !V && Nx >= 4 && is_pinned(x) && is_pinned(z) && (!P || is_pinned(P)) &&
         (!w || is_pinned(w))) {

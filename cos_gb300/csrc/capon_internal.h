@@ -68,6 +68,9 @@ int launch_format_r(const FrameDev &f, const float2 *Rhi, const float2 *Rlo, con
 bool tc_supported(const FrameDev &f, int split);
 int launch_tc_covariance(const FrameDev &f, int split, float2 *Rw, float *dl, unsigned *status, int num_sms,
                          cudaStream_t s);
+// sliding-window inverse form (Sherman-Morrison along range); f.tile carries
+// the segment length (0 = default)
+int launch_sliding_inverse(const FrameDev &f, unsigned *status, cudaStream_t s);
 // general batched LU solve, column-major A
 int launch_lu_solve(float2 *x, const float2 *A, const float2 *b, int N, int batch, cudaStream_t s);
 // fused element-space path: candidate configurations per subarray length.

@@ -41,6 +41,12 @@ extern "C" {
 #define COS_CAPON_FORM_TC_TF32   2  /* TF32 operands (rna), FP32 accumulation           */
 #define COS_CAPON_FORM_TC_BF16X3 3  /* BF16 hi/lo split, three products, FP32 accum.    */
 #define COS_CAPON_FORM_TC_TF32X3 4  /* TF32 hi/lo split, three products, FP32 accum.    */
+/* R_d^-1 carried along range by Sherman-Morrison rank-1 changes instead of a
+   factorisation per pixel (getCaponAllC.pyx:240-252 SOLVE_WOOD with the
+   updates of woodburyc.pyx:15-107): element space, L <= 32, absolute loading
+   (COS_CAPON_LOAD_ABSOLUTE, d > 0) only; no R output, no refinement, no fb.
+   A fresh build-up starts every opts.segment pixels along range.              */
+#define COS_CAPON_FORM_SLIDING_INVERSE 5
 
 #define COS_CAPON_LOAD_ELEMENT   0  /* R_d = R + d*tr(R)/L*I before any beamspace transform
                                        (reference GPU default, buildR_kernel.cu:153-154)          */
@@ -65,6 +71,8 @@ typedef struct cos_capon_opts {
                        (getCaponAllC.pyx:346-347, getCaponPy_ref.py:103-104);
                        element space runs the float-float pipeline, beamspace
                        supports Nb <= 5                                        */
+    int segment;    /* COS_CAPON_FORM_SLIDING_INVERSE: pixels along range per
+                       fresh build-up of the inverse; 0 = 8                    */
 } cos_capon_opts;
 
 /* One frame (data cube + parameters) of a device-pointer call. */

@@ -385,3 +385,172 @@ int oracle_capon_v(const float *Xd, int Nx, int Ny, int M, double regCoef, int L
     free(jobs);
     return rc;
 }
+
+/* ---- sliding-window inverse (Sherman-Morrison along range) --------------- */
+
+/*
+ * Rank-1 change of an inverse, framework/linalg/woodburyc.pyx:73-100:
+ * for A <- A + sign x x^H and B = A^-1,
+ *     B <- B - sign (B x)(x^H B) / (1 + sign x^H B x).
+ * The reference forms B x and x^H B separately (:88-90); both are formed
+ * here too.  `u` holds 2n elements.  Returns 1 + sign x^H B x (the
+ * reference raises when it is 0, :95-96; the caller checks it).
+ */
+double oracle_sm_update(cplx *B, const cplx *x, int n, int sign, cplx *u)
+{
+    cplx *Bx = u, *xB = u + n;
+    for (int i = 0; i < n; ++i) {
+        cplx s = 0, t = 0;
+        for (int j = 0; j < n; ++j) {
+            s += B[i * n + j] * x[j];
+            t += conj(x[j]) * B[j * n + i];
+        }
+        Bx[i] = s;
+        xB[i] = t;
+    }
+    cplx xBx = 0;
+    for (int i = 0; i < n; ++i) xBx += conj(x[i]) * Bx[i];
+    const cplx den = 1.0 + (double)sign * xBx;
+    const cplx f = (double)sign / den;
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) B[i * n + j] -= f * Bx[i] * xB[j];
+    return creal(den);
+}
+
+/* iterativeBuildUpRinv / iterativeBuildDownRinv (woodburyc.pyx:15-42): one
+ * rank-1 change per subarray l = 0..M-L of the row X[0..M-1], in that order. */
+double oracle_sm_row(cplx *B, const cplx *X, int M, int L, int sign, cplx *u)
+{
+    double dmin = INFINITY;
+    for (int l = 0; l + L <= M; ++l) {
+        double den = oracle_sm_update(B, X + l, L, sign, u);
+        if (den < dmin) dmin = den;
+    }
+    return dmin;
+}
+
+typedef struct {
+    const float *Xd;
+    int Nx, Ny, M, L, Navg, segment;
+    double d;
+    cplx *z, *w;
+    double *P, *den_min;
+    int x0, x1;
+} slide_job_t;
+
+static void slide_row(const float *src, int M, cplx *dst)
+{
+    for (int m = 0; m < M; ++m) dst[m] = src[2 * m] + I * src[2 * m + 1];
+}
+
+static void *slide_worker(void *arg)
+{
+    const slide_job_t *jb = (const slide_job_t *)arg;
+    const int M = jb->M, L = jb->L, T = 2 * jb->Navg + 1, Ns = M - L + 1, Npy = jb->Ny - 2 * jb->Navg;
+    const double nt = (double)Ns * T;
+    cplx *B = (cplx *)malloc(sizeof(cplx) * ((size_t)L * L + 2 * (size_t)L + 2 * (size_t)M + L));
+    if (!B) return (void *)1;
+    cplx *u = B + (size_t)L * L, *row = u + 2 * L, *xc = row + M, *ria = xc + M;
+    double dmin = INFINITY;
+    for (int bx = jb->x0; bx < jb->x1; ++bx) {
+        const float *xb = jb->Xd + (size_t)bx * jb->Ny * M * 2;
+        for (int p0 = 0; p0 < Npy; p0 += jb->segment) {
+            const int p1 = p0 + jb->segment < Npy ? p0 + jb->segment : Npy;
+            /* fresh build-up of the window of pixel p0 (woodburyc.pyx:46-70):
+             * B = I / (Ns T d), then rows p0 .. p0+2K */
+            memset(B, 0, sizeof(cplx) * (size_t)L * L);
+            for (int i = 0; i < L; ++i) B[i * L + i] = 1.0 / (nt * jb->d);
+            for (int t = p0; t < p0 + T; ++t) {
+                slide_row(xb + (size_t)t * M * 2, M, row);
+                double dm = oracle_sm_row(B, row, M, L, +1, u);
+                if (dm < dmin) dmin = dm;
+            }
+            for (int p = p0; p < p1; ++p) {
+                if (p > p0) {
+                    /* the window moves one row: row p+2K enters, row p-1 leaves
+                     * (getCaponAllC.pyx:240-252 with the rows in this order) */
+                    slide_row(xb + (size_t)(p + T - 1) * M * 2, M, row);
+                    double dm = oracle_sm_row(B, row, M, L, +1, u);
+                    if (dm < dmin) dmin = dm;
+                    slide_row(xb + (size_t)(p - 1) * M * 2, M, row);
+                    dm = oracle_sm_row(B, row, M, L, -1, u);
+                    if (dm < dmin) dmin = dm;
+                }
+                /* R_d^-1 a = Ns T B 1 (the normalisation of woodburyc.pyx:68) */
+                cplx aRia = 0;
+                for (int i = 0; i < L; ++i) {
+                    cplx s = 0;
+                    for (int j = 0; j < L; ++j) s += B[i * L + j];
+                    ria[i] = nt * s;
+                    aRia += ria[i];
+                }
+                /* subarray sums of the centre row (getCaponC.pyx:246-255) */
+                slide_row(xb + (size_t)(p + jb->Navg) * M * 2, M, xc);
+                cplx zz = 0;
+                for (int i = 0; i < L; ++i) {
+                    cplx g = 0;
+                    for (int s = 0; s < Ns; ++s) g += xc[i + s];
+                    g /= (double)Ns;
+                    const cplx wi = ria[i] / aRia;
+                    zz += conj(wi) * g;
+                    if (jb->w) jb->w[((size_t)bx * Npy + p) * L + i] = wi;
+                }
+                jb->z[(size_t)bx * Npy + p] = zz;
+                if (jb->P) jb->P[(size_t)bx * Npy + p] = 1.0 / creal(aRia);
+            }
+        }
+    }
+    if (jb->den_min) *jb->den_min = dmin;
+    free(B);
+    return NULL;
+}
+
+/*
+ * Capon with R_d^-1 tracked along range by rank-1 changes instead of a
+ * factorisation per pixel: the SOLVE_WOOD branch of
+ * framework/beamformer/capon/getCaponAllC.pyx:240-252 with the updates of
+ * framework/linalg/woodburyc.pyx:15-107.
+ *   * Loading is absolute on the normalised covariance, R_d = R + d I, so that
+ *     A = sum x x^H + Ns T d I and R_d^-1 = Ns T A^-1 (the build-up starts
+ *     from (1/loading) I and scales by Ns T at the end, woodburyc.pyx:57-68).
+ *   * Every `segment` pixels along range start from a fresh build-up; between
+ *     two pixels row p+2K enters and row p-1 leaves.  (The reference branch
+ *     builds only at y == 0, which its range loop never reaches for Navg > 0,
+ *     and applies the entering row as a downdate; both are corrected here.)
+ *   * Outputs as the element-space path: w = R_d^-1 a / a^H R_d^-1 a,
+ *     z = sum conj(w) g, P = 1 / Re(a^H R_d^-1 a).
+ * den_min (optional, one per thread) receives the smallest Sherman-Morrison
+ * denominator seen.  Returns 0, 1 (invalid arguments) or 2 (allocation).
+ */
+int oracle_capon_sliding(const float *Xd, int Nx, int Ny, int M, double d, int L, int Navg, int segment,
+                         cplx *z, cplx *w, double *P, double *den_min, int nthreads)
+{
+    if (Nx < 1 || Ny < 1 || L < 1 || M < 1 || Navg < 0 || L > M || 2 * Navg >= Ny || segment < 1 || !(d > 0) ||
+        !Xd || !z)
+        return 1;
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > Nx) nthreads = Nx;
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * nthreads);
+    slide_job_t *jobs = (slide_job_t *)malloc(sizeof(slide_job_t) * nthreads);
+    double *dm = (double *)malloc(sizeof(double) * nthreads);
+    if (!th || !jobs || !dm) { free(th); free(jobs); free(dm); return 2; }
+    int rc = 0;
+    for (int i = 0; i < nthreads; ++i) {
+        slide_job_t j = {Xd, Nx, Ny, M, L, Navg, segment, d, z, w, P, &dm[i],
+                         (int)((long)Nx * i / nthreads), (int)((long)Nx * (i + 1) / nthreads)};
+        jobs[i] = j;
+        pthread_create(&th[i], NULL, slide_worker, &jobs[i]);
+    }
+    double dmin = INFINITY;
+    for (int i = 0; i < nthreads; ++i) {
+        void *ret = NULL;
+        pthread_join(th[i], &ret);
+        if (ret) rc = 2;
+        else if (dm[i] < dmin) dmin = dm[i];
+    }
+    if (den_min) *den_min = dmin;
+    free(th);
+    free(jobs);
+    free(dm);
+    return rc;
+}

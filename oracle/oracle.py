@@ -51,6 +51,12 @@ def lib() -> C.CDLL:
             getattr(L, name).argtypes = [vp, vp, i, vp]
         L.oracle_solve_cholesky.argtypes = [vp, vp, i, vp, vp]
         L.oracle_butler.argtypes = [i, i, vp]
+        L.oracle_sm_update.argtypes = [vp, vp, i, i, vp]
+        L.oracle_sm_update.restype = d
+        L.oracle_sm_row.argtypes = [vp, vp, i, i, i, vp]
+        L.oracle_sm_row.restype = d
+        L.oracle_capon_sliding.argtypes = [vp, i, i, i, d, i, i, i, vp, vp, vp, vp, i]
+        L.oracle_capon_sliding.restype = i
         L.oracle_butler_layout.argtypes = [i, i, vp, i]
         _lib = L
     return _lib
@@ -83,6 +89,38 @@ def capon(Xd, regCoef, L, Navg, Nb=0, bs_loading=False, fp32_scalars=True, want_
                               _p(out["w"]), _p(out["P"]), _p(out["R"]), int(nthreads))
     if rc != 0:
         raise ValueError(f"oracle_capon returned {rc}")
+    return out
+
+
+def sm_row(B, X, L, sign) -> tuple:
+    """One row of rank-1 changes of an inverse, woodburyc.pyx:15-42
+    (iterativeBuildUpRinv for sign=+1, iterativeBuildDownRinv for -1).
+    Returns (new B, smallest denominator)."""
+    B = np.array(B, dtype=np.complex128, order="C")
+    X = np.ascontiguousarray(X, dtype=np.complex128)
+    u = np.zeros(2 * L, np.complex128)
+    den = lib().oracle_sm_row(_p(B), _p(X), X.shape[0], int(L), int(sign), _p(u))
+    return B, den
+
+
+def capon_sliding(Xd, d, L, Navg, segment, want_w=True, nthreads=1) -> dict:
+    """Capon with the inverse tracked along range by Sherman-Morrison updates
+    (getCaponAllC.pyx:240-252, woodburyc.pyx:15-107), absolute loading
+    R_d = R + d I, a fresh build-up every `segment` pixels."""
+    Xd = np.ascontiguousarray(Xd, dtype=np.complex64)
+    Nx, Ny, M = Xd.shape
+    npy = Ny - 2 * Navg
+    out = dict(
+        z=np.zeros((Nx, npy), np.complex128),
+        P=np.zeros((Nx, npy), np.float64),
+        w=np.zeros((Nx, npy, L), np.complex128) if want_w else None,
+    )
+    dmin = np.zeros(1, np.float64)
+    rc = lib().oracle_capon_sliding(_p(Xd), Nx, Ny, M, float(d), int(L), int(Navg), int(segment), _p(out["z"]),
+                                    _p(out["w"]), _p(out["P"]), _p(dmin), int(nthreads))
+    if rc != 0:
+        raise ValueError(f"oracle_capon_sliding returned {rc}")
+    out["den_min"] = float(dmin[0])
     return out
 
 

@@ -12,6 +12,12 @@ Writes
   ``setUp`` with ``ast``: the 3x3 real and complex Hermitian matrices with
   their Cholesky factors, right-hand sides and solutions, the 3x3 / 4x4
   Butler matrices and the 2x3 beamspace transform of ``complexb``.
+* ``woodbury_ref_cases.npz`` -- rank-1 updates and downdates of an inverse by
+  the reference's framework/linalg/woodburyc.pyx (iterativeBuildUpRinv /
+  iterativeBuildDownRinv) on seeded rows, and a small sliding-window Capon
+  case driven by those two functions (the reference's own build-up,
+  iterativeBuildRinv, seeds with a real-typed identity that its complex
+  buffer declaration rejects, so the build-up here starts from a complex one).
 * ``capon_ref_cases.npz`` -- seeded inputs and the outputs of the
   reference's own getCaponC.getCaponCPy (z, zPow, w; complex128) for small
   cases covering K = 0, L = 1, L = M, one valid range row, and the
@@ -112,10 +118,66 @@ def ref_cases() -> dict:
     return out
 
 
+# (M, L, rows, seed) for the update / downdate cases
+WOOD_CASES = [(8, 4, 3, 20), (12, 6, 4, 21), (10, 10, 3, 22), (64, 32, 2, 23)]
+# sliding-window case: (Nx, Ny, M, L, K, d, segment, seed)
+WOOD_SLIDE = (2, 20, 12, 6, 1, 0.3, 5, 24)
+
+
+def woodbury_cases() -> dict:
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ref  # noqa: E402
+    ref._prepare()
+    from framework.linalg import woodburyc as wb  # noqa: E402
+    out = {"cases": np.array(WOOD_CASES, dtype=np.int64)}
+    for i, (M, L, n, seed) in enumerate(WOOD_CASES):
+        rng = np.random.default_rng(seed)
+        G = rng.standard_normal((L, 2 * L)) + 1j * rng.standard_normal((L, 2 * L))
+        B0 = np.linalg.inv(G @ G.conj().T / (2 * L) + 0.5 * np.eye(L))
+        X = rng.standard_normal((n, M)) + 1j * rng.standard_normal((n, M))
+        B = B0.copy()
+        ups = []
+        for r in range(n):
+            B = wb.iterativeBuildUpRinv(B, X[r], M, L)
+            ups.append(B)
+        down = wb.iterativeBuildDownRinv(B, X[0], M, L)
+        out[f"B0_{i}"], out[f"X_{i}"] = B0, X
+        out[f"up_{i}"], out[f"down_{i}"] = np.array(ups), down
+    # sliding-window Capon driven by the reference's update functions
+    Nx, Ny, M, L, K, d, seg, seed = WOOD_SLIDE
+    rng = np.random.default_rng(seed)
+    x = (rng.standard_normal((Nx, Ny, M)) + 1j * rng.standard_normal((Nx, Ny, M))).astype(np.complex64)
+    x += (3.0 * np.exp(1j * 0.9 * np.arange(M))[None, None, :]).astype(np.complex64)
+    T, Ns, npy = 2 * K + 1, M - L + 1, Ny - 2 * K
+    xd = x.astype(np.complex128)
+    z = np.zeros((Nx, npy), complex)
+    P = np.zeros((Nx, npy))
+    w = np.zeros((Nx, npy, L), complex)
+    for bx in range(Nx):
+        for p0 in range(0, npy, seg):
+            B = np.eye(L, dtype=complex) / (Ns * T * d)
+            for t in range(p0, p0 + T):
+                B = wb.iterativeBuildUpRinv(B, xd[bx, t], M, L)
+            for p in range(p0, min(p0 + seg, npy)):
+                if p > p0:
+                    B = wb.iterativeBuildUpRinv(B, xd[bx, p + T - 1], M, L)
+                    B = wb.iterativeBuildDownRinv(B, xd[bx, p - 1], M, L)
+                ria = Ns * T * B.sum(axis=1)
+                aria = ria.sum()
+                g = np.array([xd[bx, p + K, i:i + Ns].sum() / Ns for i in range(L)])
+                w[bx, p] = ria / aria
+                z[bx, p] = np.sum(w[bx, p].conj() * g)
+                P[bx, p] = 1.0 / aria.real
+    out["slide_params"] = np.array(WOOD_SLIDE, dtype=np.float64)
+    out["slide_x"], out["slide_z"], out["slide_P"], out["slide_w"] = x, z, P, w
+    return out
+
+
 def main() -> None:
     np.savez_compressed(os.path.join(HERE, "linalg_known_answers.npz"), **known_answers())
     np.savez_compressed(os.path.join(HERE, "capon_ref_cases.npz"), **ref_cases())
-    for f in ("linalg_known_answers.npz", "capon_ref_cases.npz"):
+    np.savez_compressed(os.path.join(HERE, "woodbury_ref_cases.npz"), **woodbury_cases())
+    for f in ("linalg_known_answers.npz", "capon_ref_cases.npz", "woodbury_ref_cases.npz"):
         print(f, os.path.getsize(os.path.join(HERE, f)), "bytes")
 
 

@@ -98,3 +98,26 @@ def test_steering_time_axis_must_be_uniform():
         tdib._axis(np.array([0.0, 1.0, 3.0]))
     with pytest.raises(ValueError):
         tdib._axis(np.array([1.0]))
+
+
+def test_struct_layouts_match_the_header(libmod, tmp_path):
+    # sizeof / offsetof of every struct of the header, compiled by the C
+    # compiler, against the ctypes mirrors the Python side passes
+    structs = {"cos_capon_opts": libmod.Opts, "cos_capon_frame": libmod.Frame,
+               "cos_capon_adjoint": libmod.Adjoint}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", f'#include "{HEADER}"', "int main(void) {"]
+    for cname, cls in structs.items():
+        lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')
+        for fname, _ in cls._fields_:
+            lines.append(f'printf("{cname}.{fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["return 0;", "}"]
+    src, exe = tmp_path / "layout.c", tmp_path / "layout"
+    src.write_text("\n".join(lines))
+    import subprocess
+    subprocess.run(["gcc", "-std=c11", str(src), "-o", str(exe)], check=True)
+    got = dict(l.split() for l in subprocess.run([str(exe)], check=True, capture_output=True,
+                                                 text=True).stdout.splitlines())
+    for cname, cls in structs.items():
+        assert int(got[cname]) == C.sizeof(cls), cname
+        for fname, _ in cls._fields_:
+            assert int(got[f"{cname}.{fname}"]) == getattr(cls, fname).offset, f"{cname}.{fname}"

@@ -229,3 +229,50 @@ def test_general_subspace_matches_numpy_restatement():
                 wb = Ria / aRia
                 np.testing.assert_allclose(o["z"][b, p], np.vdot(wb, V @ g), rtol=1e-9)
                 np.testing.assert_allclose(o["P"][b, p], 1.0 / aRia.real, rtol=1e-9)
+
+
+WOOD = np.load(os.path.join(GOLD, "woodbury_ref_cases.npz"))
+
+
+@pytest.mark.parametrize("i", range(len(WOOD["cases"])))
+def test_sherman_morrison_matches_reference_woodbury(i):
+    # iterativeBuildUpRinv / iterativeBuildDownRinv (woodburyc.pyx:15-42) outputs
+    M, L, n, _ = (int(v) for v in WOOD["cases"][i])
+    B, X = WOOD[f"B0_{i}"], WOOD[f"X_{i}"]
+    for r in range(n):
+        B, den = oracle.sm_row(B, X[r], L, +1)
+        assert den > 1.0
+        np.testing.assert_allclose(B, WOOD[f"up_{i}"][r], rtol=0, atol=1e-13 * np.abs(B).max())
+    Bd, _ = oracle.sm_row(B, X[0], L, -1)
+    np.testing.assert_allclose(Bd, WOOD[f"down_{i}"], rtol=0, atol=1e-12 * np.abs(Bd).max())
+
+
+def test_sliding_inverse_matches_reference_woodbury_driver():
+    # the sliding-window Capon case computed with the reference's own update functions
+    Nx, Ny, M, L, K, d, seg, _ = WOOD["slide_params"]
+    o = oracle.capon_sliding(WOOD["slide_x"], float(d), int(L), int(K), int(seg))
+    np.testing.assert_allclose(o["P"], WOOD["slide_P"], rtol=1e-12)
+    np.testing.assert_allclose(o["w"], WOOD["slide_w"], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(o["z"], WOOD["slide_z"], rtol=0, atol=1e-12 * np.abs(WOOD["slide_z"]).max())
+
+
+@pytest.mark.parametrize("seg", [1, 6, 10_000])
+def test_sliding_inverse_equals_direct_solve(seg):
+    # in FP64 the tracked inverse and a Cholesky solve per pixel agree
+    # (absolute loading), whatever the segment length
+    rng = np.random.default_rng(31)
+    x = (rng.standard_normal((3, 60, 32)) + 1j * rng.standard_normal((3, 60, 32))).astype(np.complex64)
+    x += (5.0 * np.exp(1j * 0.4 * np.arange(32))[None, None, :]).astype(np.complex64)
+    a = oracle.capon_sliding(x, 0.2, 16, 1, seg)
+    b = oracle.capon(x, 0.2, 16, 1, absolute=True, fp32_scalars=False)
+    np.testing.assert_allclose(a["P"], b["P"], rtol=1e-10)
+    np.testing.assert_allclose(a["w"], b["w"], rtol=0, atol=1e-10)
+    np.testing.assert_allclose(a["z"], b["z"], rtol=0, atol=1e-10 * np.abs(b["z"]).max())
+    assert a["den_min"] > 0.0
+
+
+def test_sliding_inverse_rejects_invalid():
+    x = np.zeros((1, 10, 8), np.complex64)
+    for args in ((0.2, 4, 1, 0), (0.0, 4, 1, 3), (0.2, 9, 1, 3), (0.2, 4, 5, 3)):
+        with pytest.raises(ValueError):
+            oracle.capon_sliding(x, *args)
