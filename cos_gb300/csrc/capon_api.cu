@@ -58,7 +58,6 @@ struct cos_capon_ctx {
     // stage entry points
     DevBuf A, b, sol;
     DevBuf V;           // subspace matrix of the host-pointer subspace call
-    DevBuf wr_scratch;  // Cholesky rows parked by the fused w/R instantiation
     DevBuf tdib_in;     // inputs of the host-pointer steering call
     DevBuf lca_pw;      // |Z|^2 planes of the LCA selection
     // autotuner: chosen fused candidate per (L, K, M, w-or-R requested)
@@ -312,12 +311,6 @@ static int run_frames(cos_capon_ctx *c, const FrameDev *fs, int n, const cos_cap
                 fp.f[fp.n++] = fs[j];
                 ++j;
             }
-            if (wr) {
-                const size_t need = fused_wr_scratch_bytes(f.L, c->num_sms);
-                if (int e = c->wr_scratch.ensure(need)) return e;
-                fp.wr_scratch = (float2 *)c->wr_scratch.p;
-                fp.wr_scratch_bytes = c->wr_scratch.cap;
-            }
             int e = launch_fused_tuned(c, fp, wr, s);
             if (e) return e;
             i = j;
@@ -398,7 +391,7 @@ int cos_capon_destroy(cos_capon_ctx *c)
     if (!c) return COS_CAPON_ERR_INVALID_VALUE;
     cudaStreamSynchronize(c->stream);
     for (DevBuf *b : {&c->x, &c->z, &c->P, &c->w, &c->R, &c->Rwork, &c->Rlo, &c->dl, &c->Ria, &c->A, &c->b,
-                      &c->sol, &c->V, &c->tdib_in, &c->lca_pw, &c->wr_scratch})
+                      &c->sol, &c->V, &c->tdib_in, &c->lca_pw})
         b->release();
     if (c->d_status) cudaFree(c->d_status);
     if (c->stream) cudaStreamDestroy(c->stream);

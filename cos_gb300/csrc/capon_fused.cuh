@@ -129,9 +129,6 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int gi = lane / G, r = lane % G;
     const int nthreads = C::WARPS * 32;
-    // WR: slot (i, m) of this thread's part of U lives at ubase[(i*NM + m) * nthreads];
-    // the constant stride keeps every access at an immediate offset of one pointer
-    float2 *const ubase = WR ? fp.wr_scratch + (size_t)blockIdx.x * (L * NM * nthreads) + tid : nullptr;
 
     // all frames of one launch share K and M bounds through the first frame's
     // carve-up; the host groups frames so that K and M are equal within a launch
@@ -456,11 +453,6 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
                 for (int m = 0; m < NM; ++m)
                     if (m >= mi) rb[m * G + r] = nq[m];
                 __syncwarp();
-                if (WR) {   // row i of U is final: park it for the back substitution
-#pragma unroll
-                    for (int m = 0; m < NM; ++m)
-                        if (m >= mi) ubase[(i * NM + m) * nthreads] = A[i][m];
-                }
                 // right-hand sides, rows m*G + r > i:  b -= conj(U[i,row]) * y
                 // (for m > mi every row of the slot is below i; for m = mi only r > i%G)
                 {
@@ -529,19 +521,15 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
 #pragma unroll
                 for (int i = L - 1; i >= 0; --i) {
                     const int oi = i % G, mi = i / G;
-                    float2 Ui[NM];
-#pragma unroll
-                    for (int m = 0; m < NM; ++m)
-                        Ui[m] = m >= mi ? ubase[(i * NM + m) * nthreads] : make_float2(0.f, 0.f);
                     float2 part = make_float2(0.f, 0.f);
 #pragma unroll
                     for (int m = 0; m < NM; ++m)
-                        if (m >= mi && m * G + r > i) part = cadd(part, cmul(Ui[m], xv[m]));
+                        if (m >= mi && m * G + r > i) part = cadd(part, cmul(A[i][m], xv[m]));
 #pragma unroll
                     for (int o = G / 2; o; o >>= 1) part = cadd(part, shfl2_xor(part, o, G));
                     if (r == oi) {
                         const float2 num = csub(b1[mi], part);
-                        xv[mi] = cscale(num, 1.0f / Ui[mi].x);
+                        xv[mi] = cscale(num, 1.0f / A[i][mi].x);
                     }
                 }
                 if (active) {
@@ -556,13 +544,6 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
 }
 
 // ---- launch helper ---------------------------------------------------------
-// U slots per block of the WR instantiation
-template <class C>
-constexpr size_t L_SLOTS()
-{
-    return (size_t)C::L * C::NM * C::WARPS * 32;
-}
-
 template <class C, bool WR>
 int launch_cfg(FramesParam fp, unsigned *status, int num_sms, cudaStream_t s)
 {
@@ -589,8 +570,6 @@ int launch_cfg(FramesParam fp, unsigned *status, int num_sms, cudaStream_t s)
     if (per_sm < 1) return cudaErrorNotSupported;
     long long grid = (long long)num_sms * per_sm;
     if (grid > begin) grid = begin;
-    if (WR && (!fp.wr_scratch || fp.wr_scratch_bytes < (size_t)grid * L_SLOTS<C>() * sizeof(float2)))
-        return cudaErrorMemoryAllocation;
     fused_kernel<C, WR><<<(unsigned)grid, C::WARPS * 32, S.total, s>>>(fp, begin, status);
     return cudaGetLastError();
 }

@@ -31,18 +31,7 @@ static constexpr int kMaxFrames = 8;
 struct FramesParam {
     FrameDev f[kMaxFrames];
     int n;
-    // the fused instantiation that writes w parks each finished row of the
-    // Cholesky factor here (per block [slot][thread], L2-resident) until the
-    // back substitution, instead of holding all of U in registers
-    float2 *wr_scratch;
-    size_t wr_scratch_bytes;
 };
-// scratch the context reserves for a fused w/R launch of subarray length L
-// (two resident blocks per SM at most, 4 column slots per lane, 256 threads)
-inline size_t fused_wr_scratch_bytes(int L, int num_sms)
-{
-    return (size_t)num_sms * 2 * (size_t)L * 4 * 256 * 8;
-}
 
 // Error bits written to the device status word.
 enum : unsigned { ERR_TIMEOUT = 1u, ERR_NOT_PD = 2u };
