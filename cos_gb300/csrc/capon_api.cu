@@ -303,6 +303,8 @@ static int run_frames(cos_capon_ctx *c, const FrameDev *fs, int n, const cos_cap
         if (use_fused(f, o)) {
             FramesParam fp;
             memset(&fp, 0, sizeof(fp));
+            const char *stall = getenv("COS_CAPON_TEST_STALL");
+            fp.stall_test = stall && stall[0] == '1';
             bool wr = false;
             int j = i;
             while (j < n && fp.n < kMaxFrames && use_fused(fs[j], o) && fs[j].L == f.L && fs[j].K == f.K &&

@@ -55,9 +55,9 @@ COS_DEV bool mbar_try_wait(uint64_t *bar, uint32_t phase)
     return ok != 0;
 }
 // bounded wait; false when the limit was reached
-COS_DEV bool mbar_wait_bounded(uint64_t *bar, uint32_t phase)
+COS_DEV bool mbar_wait_bounded(uint64_t *bar, uint32_t phase, uint32_t limit = kWaitLimit)
 {
-    for (uint32_t it = 0; it < kWaitLimit; ++it)
+    for (uint32_t it = 0; it < limit; ++it)
         if (mbar_try_wait(bar, phase)) return true;
     return false;
 }
@@ -68,6 +68,25 @@ COS_DEV void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
             smem_addr(dst)),
         "l"(src), "r"(bytes), "r"(smem_addr(bar))
         : "memory");
+}
+// timeout exit of thread 0: record it, then wait (bounded) for the bulk copies
+// still in flight into this CTA's shared memory -- buffer b (whose phase bit
+// was already flipped) and, when a next unit was issued, buffer b^1 -- so
+// that none lands after the CTA has left.  Kept out of line, away from the
+// register allocation of the unit loop.
+static __device__ __noinline__ void timeout_exit(unsigned *status, uint64_t *bar, int b, uint32_t ph0, uint32_t ph1,
+                                          bool next_issued)
+{
+    atomicOr(status, ERR_TIMEOUT);
+    mbar_wait_bounded(&bar[b], (b ? ph1 : ph0) ^ 1u);
+    if (next_issued) mbar_wait_bounded(&bar[b ^ 1], b ? ph0 : ph1);
+}
+// test of the timeout path (thread 0): a bounded wait on barrier 2, which
+// nothing completes, runs out; record it, let the first unit's copy land, leave
+static __device__ __noinline__ void stall_test_exit(unsigned *status, uint64_t *bar, bool first_issued)
+{
+    if (!mbar_wait_bounded(&bar[2], 0u, kStallTestLimit)) atomicOr(status, ERR_TIMEOUT);
+    if (first_issued) mbar_wait_bounded(&bar[0], 0u);
 }
 COS_DEV void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 COS_DEV void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
@@ -145,6 +164,7 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
     if (tid == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
+        mbar_init(&bar[2], 1);  // never arrived on: the stall test waits here
         fence_mbar_init();
     }
     __syncthreads();
@@ -171,6 +191,10 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
     long long u = blockIdx.x;
     uint32_t ph0 = 0u, ph1 = 0u;
     if (tid == 0 && u < total_units) issue(u, 0);
+    if (fp.stall_test) {
+        if (tid == 0) stall_test_exit(status, bar, u < total_units);
+        return;
+    }
     int b = 0;
     for (; u < total_units; u += gridDim.x, b ^= 1) {
         const long long un = u + gridDim.x;
@@ -187,7 +211,7 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
         const bool ok = mbar_wait_bounded(&bar[b], b ? ph1 : ph0);
         if (b) ph1 ^= 1u; else ph0 ^= 1u;
         if (__syncthreads_or(!ok)) {
-            if (tid == 0) atomicOr(status, ERR_TIMEOUT);
+            if (tid == 0) timeout_exit(status, bar, b, ph0, ph1, u + gridDim.x < total_units);
             return;
         }
         const float2 *src = f.x + ((size_t)bx * f.Ny + p0) * M;

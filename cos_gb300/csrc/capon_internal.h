@@ -31,6 +31,10 @@ static constexpr int kMaxFrames = 8;
 struct FramesParam {
     FrameDev f[kMaxFrames];
     int n;
+    // nonzero: every CTA waits on a barrier that nothing completes, so the
+    // bounded wait runs out and the launch reports ERR_TIMEOUT (the test of
+    // the timeout path; set from COS_CAPON_TEST_STALL, never by default)
+    int stall_test;
 };
 
 // Error bits written to the device status word.
@@ -39,6 +43,8 @@ enum : unsigned { ERR_TIMEOUT = 1u, ERR_NOT_PD = 2u };
 // Bounded wait on a shared-memory mbarrier phase; returns false after
 // `limit` polls (the caller records ERR_TIMEOUT and leaves).
 static constexpr uint32_t kWaitLimit = 1u << 22;
+// polls of the stall test's wait (a few milliseconds)
+static constexpr uint32_t kStallTestLimit = 1u << 12;
 
 // ---- launchers (return cudaError_t as int) ----------------------------------
 // plain three-stage element-space pipeline; R_work must hold Nx*Npy*L*L complex

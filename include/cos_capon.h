@@ -30,6 +30,12 @@ extern "C" {
                                             BuildR.cpp:37-48, Solver.cpp:34-42)                    */
 #define COS_CAPON_ERR_NOT_SUPPORTED 801  /* cudaErrorNotSupported: option outside what is built     */
 #define COS_CAPON_ERR_TIMEOUT       909  /* cudaErrorTimeout: a bounded device-side wait expired   */
+/* Every device-side wait is bounded; on expiry the kernel records the timeout,
+   lets its own bulk copies land and returns, so the context stays usable and
+   the call returns 909 (that call's outputs are undefined).  With the
+   environment variable COS_CAPON_TEST_STALL=1 the fused kernel waits on a
+   barrier that nothing completes, so the timeout path can be tested without a
+   device fault. */
 
 /* ---- options ------------------------------------------------------------ */
 #define COS_CAPON_FORM_FUSED   0  /* one fused persistent kernel per launch (default)             */
