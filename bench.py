@@ -66,21 +66,27 @@ def _peaks() -> dict:
 
 
 class Clocks:
-    """nvidia-smi sampling during the timed region."""
+    """nvidia-smi sampling around the timed region.  The sampler starts before
+    the warm-up, polls every 20 ms and stamps each sample with nvidia-smi's own
+    clock; `window(t0, t1)` marks the timed region (time.time() bounds), and
+    the summary keeps the samples inside it -- or, when the region is shorter
+    than one polling interval, the samples of the whole sampled span, and says
+    so."""
 
     def __init__(self, dev: int):
-        self.dev, self.proc, self.out = dev, None, []
+        self.dev, self.proc, self.out, self.win = dev, None, [], None
 
     def __enter__(self):
-        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+        q = ("timestamp,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
              "clocks_event_reasons.sw_power_cap")
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), f"--query-gpu={q}",
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            time.sleep(0.3)   # nvidia-smi start-up, so that sampling covers the warm-up and the timed region
         except OSError:
             self.proc = None
         return self
@@ -89,29 +95,44 @@ class Clocks:
         for line in self.proc.stdout:
             self.out.append(line.strip())
 
+    def window(self, t0: float, t1: float):
+        self.win = (t0, t1)
+
     def __exit__(self, *a):
         if self.proc:
+            time.sleep(0.05)
             self.proc.terminate()
             self.proc.wait()
             self.t.join(timeout=2)
 
+    @staticmethod
+    def _stamp(s: str):
+        import datetime
+        for fmt in ("%Y/%m/%d %H:%M:%S.%f", "%Y/%m/%d %H:%M:%S"):
+            try:
+                return datetime.datetime.strptime(s, fmt).timestamp()
+            except ValueError:
+                pass
+        return None
+
     def summary(self) -> dict:
-        sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        rows = []
         for line in self.out:
             f = [v.strip() for v in line.split(",")]
-            if len(f) < 7:
+            if len(f) < 8:
                 continue
             try:
-                sm.append(float(f[0]))
-                mx = float(f[1])
+                rows.append((self._stamp(f[0]), float(f[1]), float(f[2]), f[4:8]))
             except ValueError:
                 continue
-            for n, v in zip(names, f[3:7]):
-                if v.lower() == "active":
-                    reasons.add(n)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "samples": len(sm),
-                "reasons": sorted(reasons)}
+        inside = [r for r in rows if self.win and r[0] is not None and self.win[0] <= r[0] <= self.win[1]]
+        use, span = (inside, "timed region") if inside else (rows, "warm-up and timed region (region shorter "
+                                                                   "than the 20 ms polling interval)")
+        reasons = sorted({n for r in use for n, v in zip(names, r[3]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median([r[1] for r in use]) if use else None,
+                "sm_max_mhz": use[-1][2] if use else None, "samples": len(use), "span": span,
+                "reasons": reasons}
 
 
 def fp32_peak_tflops(torch) -> float:
@@ -228,7 +249,7 @@ def run_gpu(args) -> None:
                               P=torch.empty((NX, npy), dtype=torch.float32, device="cuda"))
         return f
 
-    def time_form(form: int, steps: int, warmup: int):
+    def time_form(form: int, steps: int, warmup: int, clk=None):
         f = frame()
         o = capon.opts(form=form)
         with torch.cuda.stream(stream):
@@ -238,6 +259,7 @@ def run_gpu(args) -> None:
         replicas.barrier(dist)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.time()
         with torch.cuda.stream(stream):
             e0.record(stream)
             for _ in range(steps):
@@ -245,12 +267,14 @@ def run_gpu(args) -> None:
             e1.record(stream)
         e1.synchronize()
         torch.cuda.synchronize()
+        if clk is not None:
+            clk.window(t0, time.time())
         ms = replicas.max_over_ranks(dist, e0.elapsed_time(e1) / steps, device="cuda")
         return ms, f
 
     # fused (headline), with clocks sampled during the timed region
     with Clocks(local) as clk:
-        ms, f = time_form(_lib.FORM_FUSED, args.steps, args.warmup)
+        ms, f = time_form(_lib.FORM_FUSED, args.steps, args.warmup, clk)
     clocks = clk.summary()
     value = replicas.aggregate_rate(NPIX, ms, world)
 

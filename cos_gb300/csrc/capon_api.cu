@@ -139,7 +139,7 @@ static bool use_fused(const FrameDev &f, const cos_capon_opts &o)
     const FusedCandidate *c = nullptr;
     const int n = candidates(f.L, f.K, &c);
     for (int i = 0; i < n; ++i)
-        if (c[i].M == 0 || c[i].M == f.M) return true;
+        if ((c[i].M == 0 || c[i].M == f.M) && c[i].smem(f.K, f.M) <= kFusedSmemMax) return true;
     return false;
 }
 
@@ -156,11 +156,9 @@ static int launch_fused_tuned(cos_capon_ctx *c, const FramesParam &fp, bool wr, 
     const int n = candidates(f0.L, f0.K, &cand);
     std::vector<int> ok;
     for (int i = 0; i < n; ++i) {
-        bool fits = cand[i].M == 0;
-        if (!fits) {
-            fits = true;
-            for (int q = 0; q < fp.n; ++q) fits &= (fp.f[q].M == cand[i].M);
-        }
+        bool fits = true;
+        for (int q = 0; q < fp.n; ++q)
+            fits &= (cand[i].M == 0 || fp.f[q].M == cand[i].M) && cand[i].smem(fp.f[q].K, fp.f[q].M) <= kFusedSmemMax;
         if (fits) ok.push_back(i);
     }
     if (ok.empty()) return COS_CAPON_ERR_NOT_SUPPORTED;

@@ -124,7 +124,7 @@ struct Smem {
         off_c = off_xe + (((size_t)rows * XS * sizeof(float4) + 127) & ~(size_t)127);
         off_g = off_c + (((size_t)2 * rows * L * sizeof(float2) + 127) & ~(size_t)127);
         off_rb = off_g + (((size_t)TILE * L * sizeof(float2) + 127) & ~(size_t)127);
-        off_bar = off_rb + (((size_t)WARPS * PPW * (L + 1) * sizeof(float4) + 127) & ~(size_t)127);
+        off_bar = off_rb + (((size_t)2 * WARPS * PPW * (L + 1) * sizeof(float4) + 127) & ~(size_t)127);
         total = off_bar + 64;
     }
 };
@@ -158,7 +158,8 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
     float2 *cs = (float2 *)(smem + S.off_c);
     float2 *cl = cs + (size_t)S.rows * L;
     float2 *gs = (float2 *)(smem + S.off_g);
-    float4 *rb = (float4 *)(smem + S.off_rb) + (size_t)(warp * PPW + gi) * (L + 1);
+    // two pivot-row buffers per pixel group, alternating by Cholesky step
+    float4 *rb = (float4 *)(smem + S.off_rb) + (size_t)(warp * PPW + gi) * 2 * (L + 1);
     uint64_t *bar = (uint64_t *)(smem + S.off_bar);
 
     if (tid == 0) {
@@ -461,22 +462,25 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
                     b1[mi] = make_float2(b1[mi].x * inv, b1[mi].y * inv);
                     b2[mi] = make_float2(b2[mi].x * inv, b2[mi].y * inv);
                 }
-                const float2 y1 = shfl2(b1[mi], oi, G);
-                const float2 y2 = shfl2(b2[mi], oi, G);
                 // publish row i as (-Re, +Im, -Im, -Re) of U[i, j]: with the consumer's
                 // splats (vr, vr), (vi, vi) of its own U[i, j'] two packed fmas give
-                // A[k][j'] -= conj(U[i,k]) U[i,j']
+                // A[k][j'] -= conj(U[i,k]) U[i,j'].  Slot L carries (y1_i, y2_i).
+                // Step i writes buffer i&1, last read at step i-2, before the
+                // barrier that ended step i-1: one barrier per step suffices.
+                float4 *const rbi = rb + (i & 1) * (L + 1);
                 float4 nq[NM];
 #pragma unroll
                 for (int m = 0; m < NM; ++m) {
                     const float2 v = m >= mi ? A[i][m] : make_float2(0.f, 0.f);
                     nq[m] = make_float4(-v.x, v.y, -v.y, -v.x);
                 }
-                __syncwarp();
 #pragma unroll
                 for (int m = 0; m < NM; ++m)
-                    if (m >= mi) rb[m * G + r] = nq[m];
+                    if (m >= mi) rbi[m * G + r] = nq[m];
+                if (r == oi) rbi[L] = make_float4(b1[mi].x, b1[mi].y, b2[mi].x, b2[mi].y);
                 __syncwarp();
+                const float4 yy = rbi[L];
+                const float2 y1 = make_float2(yy.x, yy.y), y2 = make_float2(yy.z, yy.w);
                 // right-hand sides, rows m*G + r > i:  b -= conj(U[i,row]) * y
                 // (for m > mi every row of the slot is below i; for m = mi only r > i%G)
                 {
@@ -506,7 +510,7 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
 #pragma unroll
                 for (int k = 1; k < L; ++k) {
                     if (k > i) {
-                        const float4 u4 = rb[k];
+                        const float4 u4 = rbi[k];
 #pragma unroll
                         for (int m = 0; m < NM; ++m)
                             if (m >= k / G && m >= mi)
@@ -568,6 +572,12 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
 }
 
 // ---- launch helper ---------------------------------------------------------
+template <class C>
+size_t smem_bytes(int K, int M)
+{
+    return Smem(C::TILE, K, C::M ? C::M : M, C::L, C::WARPS, C::PPW).total;
+}
+
 template <class C, bool WR>
 int launch_cfg(FramesParam fp, unsigned *status, int num_sms, cudaStream_t s)
 {
@@ -584,7 +594,7 @@ int launch_cfg(FramesParam fp, unsigned *status, int num_sms, cudaStream_t s)
         begin += (long long)g.Nx * g.tiles_per_beam;
     }
     Smem S(C::TILE, f0.K, C::M ? C::M : f0.M, C::L, C::WARPS, C::PPW);
-    if (S.total > 227 * 1024) return cudaErrorNotSupported;
+    if (S.total > kFusedSmemMax) return cudaErrorNotSupported;
     cudaError_t e = cudaFuncSetAttribute(fused_kernel<C, WR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)S.total);
     if (e != cudaSuccess) return e;

@@ -19,9 +19,9 @@ int launch_2(const FramesParam &fp, bool wr, unsigned *st, int n, cudaStream_t s
 }
 
 const FusedCandidate kCand[] = {
-    {"L16.G4.W8.N1.sync.M32.T5", 16, 5, 32, launch_0},
-    {"L16.G4.W8.N1.M32.T5", 16, 5, 32, launch_1},
-    {"L16.G4.W8.N1.sync.T5", 16, 5, 0, launch_2},
+    {"L16.G4.W8.N1.sync.M32.T5", 16, 5, 32, launch_0, fused::smem_bytes<fused::Cfg<16, 4, 8, 1, 5, 32, true>>},
+    {"L16.G4.W8.N1.M32.T5", 16, 5, 32, launch_1, fused::smem_bytes<fused::Cfg<16, 4, 8, 1, 5, 32, false>>},
+    {"L16.G4.W8.N1.sync.T5", 16, 5, 0, launch_2, fused::smem_bytes<fused::Cfg<16, 4, 8, 1, 5, 0, true>>},
 };
 }  // namespace
 

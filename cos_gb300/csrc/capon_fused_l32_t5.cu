@@ -19,9 +19,9 @@ int launch_2(const FramesParam &fp, bool wr, unsigned *st, int n, cudaStream_t s
 }
 
 const FusedCandidate kCand[] = {
-    {"L32.G8.W8.N2.sync.M64.T5", 32, 5, 64, launch_0},
-    {"L32.G8.W8.N2.M64.T5", 32, 5, 64, launch_1},
-    {"L32.G8.W8.N2.sync.T5", 32, 5, 0, launch_2},
+    {"L32.G8.W8.N2.sync.M64.T5", 32, 5, 64, launch_0, fused::smem_bytes<fused::Cfg<32, 8, 8, 2, 5, 64, true>>},
+    {"L32.G8.W8.N2.M64.T5", 32, 5, 64, launch_1, fused::smem_bytes<fused::Cfg<32, 8, 8, 2, 5, 64, false>>},
+    {"L32.G8.W8.N2.sync.T5", 32, 5, 0, launch_2, fused::smem_bytes<fused::Cfg<32, 8, 8, 2, 5, 0, true>>},
 };
 }  // namespace
 

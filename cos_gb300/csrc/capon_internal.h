@@ -88,7 +88,11 @@ struct FusedCandidate {
     int T;  // the temporal window 2K+1 the instantiation is compiled for
     int M;  // the channel count it is compiled for, 0 = any
     int (*launch)(const FramesParam &fp, bool want_w_or_R, unsigned *status, int num_sms, cudaStream_t s);
+    size_t (*smem)(int K, int M);  // dynamic shared memory of a launch for (K, M)
 };
+// shared memory one CTA may use; a candidate whose tile needs more for a
+// frame's (K, M) is not used for it (the precise pipeline takes the frame)
+static constexpr size_t kFusedSmemMax = 227 * 1024;
 int fused_candidates_l16_t1(const FusedCandidate **out);
 int fused_candidates_l16_t3(const FusedCandidate **out);
 int fused_candidates_l16_t5(const FusedCandidate **out);

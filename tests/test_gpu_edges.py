@@ -8,7 +8,9 @@ Each case exercises a branch the config-sized tests do not reach:
   * a range count one pixel past a whole tile, so the last tile of each beam
     holds one pixel;
   * an M without a compile-time instantiation (run-time M);
-  * L = M, one subarray (Ns = 1), where R has rank <= 2K + 1 before loading.
+  * L = M, one subarray (Ns = 1), where R has rank <= 2K + 1 before loading;
+  * an M whose tile would not fit in shared memory (the frame takes the
+    precise pipeline instead of the fused kernel).
 Both the fused form (0) and the plain three-stage form (1) run every case.
 """
 import numpy as np
@@ -31,6 +33,7 @@ CASES = [
     (2, 69, 64, 32, 2, 0.01, "one pixel past a whole tile"),
     (2, 90, 48, 32, 1, 0.01, "run-time M"),
     (2, 30, 16, 16, 1, 0.1, "L = M, one subarray"),
+    (2, 40, 96, 32, 2, 0.01, "M past the fused tile's shared memory"),
 ]
 
 
