@@ -15,13 +15,15 @@
 //        R[k,j] = R[k-1,j-1] + sum_t (x_t[k-1+Ns] conj(x_t[j-1+Ns]) - x_t[k-1] conj(x_t[j-1]))
 //      with R[k-1,j-1] taken from the neighbouring lane by a shuffle;
 //   4. diagonal loading d*tr(R)/L (getCaponC.pyx:257-262);
-//   5. right-looking Cholesky U^H U = R in the same registers, the pivot row
-//      broadcast through shared memory, with the two right-hand sides a = 1 and
-//      g carried along, so y1 = U^-H a and y2 = U^-H g come out of the
-//      factorisation (matrixDecompc.pyx:19-50, linearSolvec.pyx:312-327);
+//   5. right-looking Cholesky in its square-root-free form R = L D L^H
+//      (U = D^-1/2 (D L^H) is the reference's factor, matrixDecompc.pyx:19-50)
+//      in the same registers, the pivot row broadcast through shared memory,
+//      with the two right-hand sides a = 1 and g carried along, so b1 = L^-1 a
+//      and b2 = L^-1 g come out of the factorisation (the forward solve of
+//      linearSolvec.pyx:312-327, with y = D^-1/2 b);
 //   6. outputs: a^H R^-1 a = |y1|^2, z = w^H g = y1^H y2 / |y1|^2
 //      (getCaponC.pyx:276-283), P = 1/((Ns*T) |y1|^2) for the normalised R,
-//      and, when asked, w = U^-1 y1 / |y1|^2 by back substitution
+//      and, when asked, w = R^-1 a / |y1|^2 by back substitution with D L^H
 //      (linearSolvec.pyx:330-346).
 // Arithmetic is FP32 with packed fma.rn.f32x2.
 #pragma once
@@ -445,26 +447,24 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
                 b2[m] = gs[lpc * L + m * G + r];
             }
 
-            // ---- Cholesky with the right-hand sides carried along
+            // ---- square-root-free Cholesky (R = L D L^H, rows of D L^H kept in A)
+            // with the right-hand sides carried along.  Step i leaves row i of
+            // A as row i of D L^H (unscaled: A[i][i] = d_i) and eliminates it
+            // from the rows below:
+            //   A[k][j] -= conj(A[i][k]) A[i][j] / d_i,   b_k -= conj(A[i][k]) b_i / d_i,
+            // so that b ends as L^-1 a, L^-1 g and, with y = D^-1/2 b,
+            //   a^H R^-1 a = sum_i |b1_i|^2 / d_i,   a^H R^-1 g = sum_i conj(b1_i) b2_i / d_i,
+            // the sums every lane accumulates from the published pivots.
             bool bad = false;
+            float s11 = 0.f;
+            float2 s12 = make_float2(0.f, 0.f);
 #pragma unroll
             for (int i = 0; i < L; ++i) {
                 const int oi = i % G, mi = i / G;
-                const float dv = __shfl_sync(0xffffffffu, A[i][mi].x, oi, G);
-                bad |= !(dv > 0.f);
-                const float inv = rsqrtf(dv);
-                // scale row i of the lane's columns; the owner of column i sets U_ii
-#pragma unroll
-                for (int m = 0; m < NM; ++m)
-                    if (m >= mi) A[i][m] = make_float2(A[i][m].x * inv, A[i][m].y * inv);
-                if (r == oi) {
-                    A[i][mi] = make_float2(dv * inv, 0.f);
-                    b1[mi] = make_float2(b1[mi].x * inv, b1[mi].y * inv);
-                    b2[mi] = make_float2(b2[mi].x * inv, b2[mi].y * inv);
-                }
-                // publish row i as (-Re, +Im, -Im, -Re) of U[i, j]: with the consumer's
-                // splats (vr, vr), (vi, vi) of its own U[i, j'] two packed fmas give
-                // A[k][j'] -= conj(U[i,k]) U[i,j'].  Slot L carries (y1_i, y2_i).
+                // publish row i as (-Re, +Im, -Im, -Re) of A[i, j]: with the consumer's
+                // splats (vr, vr), (vi, vi) of its own A[i, j'] / d_i two packed fmas
+                // give A[k][j'] -= conj(A[i,k]) A[i,j'] / d_i.  Slot i holds d_i in
+                // its first word; slot L carries (b1_i, b2_i).
                 // Step i writes buffer i&1, last read at step i-2, before the
                 // barrier that ended step i-1: one barrier per step suffices.
                 float4 *const rbi = rb + (i & 1) * (L + 1);
@@ -479,9 +479,14 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
                     if (m >= mi) rbi[m * G + r] = nq[m];
                 if (r == oi) rbi[L] = make_float4(b1[mi].x, b1[mi].y, b2[mi].x, b2[mi].y);
                 __syncwarp();
+                const float dv = -rbi[i].x;
                 const float4 yy = rbi[L];
-                const float2 y1 = make_float2(yy.x, yy.y), y2 = make_float2(yy.z, yy.w);
-                // right-hand sides, rows m*G + r > i:  b -= conj(U[i,row]) * y
+                bad |= !(dv > 0.f);
+                const float rdv = __fdividef(1.f, dv);
+                const float2 y1 = make_float2(yy.x * rdv, yy.y * rdv), y2 = make_float2(yy.z * rdv, yy.w * rdv);
+                s11 = fmaf(yy.x, y1.x, fmaf(yy.y, y1.y, s11));
+                s12 = cadd(s12, cconjmul(make_float2(yy.x, yy.y), y2));
+                // right-hand sides, rows m*G + r > i:  b -= conj(A[i,row]) * b_i / d_i
                 // (for m > mi every row of the slot is below i; for m = mi only r > i%G)
                 {
                     const float2 y1s = make_float2(y1.y, y1.x), y2s = make_float2(y2.y, y2.x);
@@ -497,13 +502,15 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
                         }
                     }
                 }
-                // trailing update A[k][j] -= conj(U[i,k]) U[i,j], i < k; slot (k,m) exists for m >= k/G
-                float2 vs[NM];
-#pragma unroll
-                for (int m = 0; m < NM; ++m) vs[m] = (m >= mi) ? A[i][m] : make_float2(0.f, 0.f);
+                // trailing update A[k][j] -= conj(A[i,k]) A[i,j] / d_i, i < k; slot (k,m) exists for m >= k/G
                 float2 vrr[NM], vii[NM];
 #pragma unroll
-                for (int m = 0; m < NM; ++m) { vrr[m] = make_float2(vs[m].x, vs[m].x); vii[m] = make_float2(vs[m].y, vs[m].y); }
+                for (int m = 0; m < NM; ++m) {
+                    const float2 v = (m >= mi) ? A[i][m] : make_float2(0.f, 0.f);
+                    const float vr = v.x * rdv, vi = v.y * rdv;
+                    vrr[m] = make_float2(vr, vr);
+                    vii[m] = make_float2(vi, vi);
+                }
                 // constant trip counts with compile-time conditions: loops whose
                 // bounds depend on i are otherwise not fully unrolled and the
                 // register matrix would fall back to local memory
@@ -520,19 +527,7 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
                 if (C::SYNC && (i % G) == G - 1) __syncthreads();
             }
 
-            // ---- outputs
-            float s11 = 0.f;
-            float2 s12 = make_float2(0.f, 0.f);
-#pragma unroll
-            for (int m = 0; m < NM; ++m) {
-                s11 += cabs2(b1[m]);
-                s12 = cadd(s12, cconjmul(b1[m], b2[m]));
-            }
-#pragma unroll
-            for (int o = G / 2; o; o >>= 1) {
-                s11 += __shfl_xor_sync(0xffffffffu, s11, o, G);
-                s12 = cadd(s12, shfl2_xor(s12, o, G));
-            }
+            // ---- outputs (s11, s12 are complete on every lane)
             const size_t pix = (size_t)bx * f.Npy + p;
             if (active && r == 0) {
                 const float is11 = 1.0f / s11;
@@ -542,7 +537,7 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
             if (bad && active && r == 0) atomicOr(status, ERR_NOT_PD);
 
             if (WR && f.w) {
-                // back substitution U x = y1, rows L-1 .. 0
+                // back substitution (D L^H) x = b1, rows L-1 .. 0: x = R^-1 a
                 float2 xv[NM];
 #pragma unroll
                 for (int m = 0; m < NM; ++m) xv[m] = make_float2(0.f, 0.f);
