@@ -721,7 +721,9 @@ def run_profile_case(args) -> None:
         Nx, Ny, _ = c["x"].shape
         frames.append(capon.DeviceFrame(x=torch.from_numpy(c["x"]).cuda(), L=c["L"], K=c["K"], d=c["d"],
                                         Nb=c["Nb"],
-                                        P=torch.empty((Nx, Ny - 2 * c["K"]), dtype=torch.float32, device="cuda")))
+                                        P=torch.empty((Nx, Ny - 2 * c["K"]), dtype=torch.float32, device="cuda"),
+                                        w=torch.empty((Nx, Ny - 2 * c["K"], c["L"]), dtype=torch.complex64,
+                                                      device="cuda") if args.profile_w else None))
     ctx = capon.Context()
     for _ in range(args.warmup + args.steps):
         capon.capon_frames(frames, ctx, capon.opts(form=args.profile_form))
@@ -741,6 +743,7 @@ def main() -> None:
                     help="time the reference's RealTimeCapon GPU library (oracle/build_rtc.py) on the workload")
     ap.add_argument("--profile-form", type=int, default=0, help="form of the profiling case (COS_CAPON_FORM_*)")
     ap.add_argument("--profile-workload", default="config1", choices=["config1", "config2", "config3"])
+    ap.add_argument("--profile-w", action="store_true", help="the profiling case also writes the weights w")
     ap.add_argument("--profile-nx", type=int, default=0,
                     help="profiling case: only the fused kernel, warmup+steps launches on Nx beams of the workload")
     args = ap.parse_args()

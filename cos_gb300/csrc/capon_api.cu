@@ -60,7 +60,7 @@ struct cos_capon_ctx {
     DevBuf V;           // subspace matrix of the host-pointer subspace call
     DevBuf tdib_in;     // inputs of the host-pointer steering call
     DevBuf lca_pw;      // |Z|^2 planes of the LCA selection
-    // autotuner: chosen fused candidate per (L, K, M, w-or-R requested)
+    // autotuner: chosen fused candidate per (L, K, M, FusedMode)
     std::map<std::tuple<int, int, int, int>, int> tuned;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     // second stream of the pipelined host-pointer call
@@ -143,13 +143,13 @@ static bool use_fused(const FrameDev &f, const cos_capon_opts &o)
     return false;
 }
 
-// Autotuner: the first launch of an (L, K, M, w/R) shape on a context times
+// Autotuner: the first launch of an (L, K, M, mode) shape on a context times
 // every candidate configuration on the frames themselves (each candidate
 // computes the same per-pixel arithmetic), keeps the fastest, and reruns it so
 // that the outputs are the winner's.  COS_CAPON_FUSED_CONFIG=<name> forces a
 // candidate.  While the stream is being captured into a graph no timing is
 // possible, so an untuned shape then takes the first candidate.
-static int launch_fused_tuned(cos_capon_ctx *c, const FramesParam &fp, bool wr, cudaStream_t s)
+static int launch_fused_tuned(cos_capon_ctx *c, const FramesParam &fp, int mode, cudaStream_t s)
 {
     const FrameDev &f0 = fp.f[0];
     const FusedCandidate *cand = nullptr;
@@ -164,25 +164,25 @@ static int launch_fused_tuned(cos_capon_ctx *c, const FramesParam &fp, bool wr, 
     if (ok.empty()) return COS_CAPON_ERR_NOT_SUPPORTED;
     if (const char *force = getenv("COS_CAPON_FUSED_CONFIG")) {
         for (int i : ok)
-            if (!strcmp(force, cand[i].name)) return cand[i].launch(fp, wr, c->d_status, c->num_sms, s);
+            if (!strcmp(force, cand[i].name)) return cand[i].launch(fp, mode, c->d_status, c->num_sms, s);
     }
-    const auto key = std::make_tuple(f0.L, f0.K, f0.M, (int)wr);
+    const auto key = std::make_tuple(f0.L, f0.K, f0.M, mode);
     auto it = c->tuned.find(key);
-    if (it != c->tuned.end()) return cand[it->second].launch(fp, wr, c->d_status, c->num_sms, s);
+    if (it != c->tuned.end()) return cand[it->second].launch(fp, mode, c->d_status, c->num_sms, s);
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone || ok.size() == 1)
-        return cand[ok[0]].launch(fp, wr, c->d_status, c->num_sms, s);
+        return cand[ok[0]].launch(fp, mode, c->d_status, c->num_sms, s);
     if (!c->ev0) {
         if (cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) {
             cudaGetLastError();
-            return cand[ok[0]].launch(fp, wr, c->d_status, c->num_sms, s);
+            return cand[ok[0]].launch(fp, mode, c->d_status, c->num_sms, s);
         }
     }
     int best = ok[0];
     float best_ms = 1e30f;
     for (int i : ok) {
         // one untimed launch, then the best of two timed ones
-        int e = cand[i].launch(fp, wr, c->d_status, c->num_sms, s);
+        int e = cand[i].launch(fp, mode, c->d_status, c->num_sms, s);
         if (e == cudaErrorNotSupported) {
             cudaGetLastError();
             continue;
@@ -191,7 +191,7 @@ static int launch_fused_tuned(cos_capon_ctx *c, const FramesParam &fp, bool wr, 
         float ms = 1e30f;
         for (int rep = 0; rep < 2; ++rep) {
             cudaEventRecord(c->ev0, s);
-            if ((e = cand[i].launch(fp, wr, c->d_status, c->num_sms, s))) return e;
+            if ((e = cand[i].launch(fp, mode, c->d_status, c->num_sms, s))) return e;
             cudaEventRecord(c->ev1, s);
             if (cudaEventSynchronize(c->ev1) != cudaSuccess) return cudaGetLastError();
             float t = 0.f;
@@ -205,9 +205,9 @@ static int launch_fused_tuned(cos_capon_ctx *c, const FramesParam &fp, bool wr, 
         }
     }
     c->tuned[key] = best;
-    if (getenv("COS_CAPON_TUNE_VERBOSE")) fprintf(stderr, "[cos_capon] L=%d K=%d M=%d wr=%d -> %s (%.3f ms)\n",
-                                                  f0.L, f0.K, f0.M, (int)wr, cand[best].name, best_ms);
-    return cand[best].launch(fp, wr, c->d_status, c->num_sms, s);
+    if (getenv("COS_CAPON_TUNE_VERBOSE")) fprintf(stderr, "[cos_capon] L=%d K=%d M=%d mode=%d -> %s (%.3f ms)\n",
+                                                  f0.L, f0.K, f0.M, mode, cand[best].name, best_ms);
+    return cand[best].launch(fp, mode, c->d_status, c->num_sms, s);
 }
 
 // plain three-stage pipeline for one element-space frame
@@ -303,15 +303,21 @@ static int run_frames(cos_capon_ctx *c, const FrameDev *fs, int n, const cos_cap
             memset(&fp, 0, sizeof(fp));
             const char *stall = getenv("COS_CAPON_TEST_STALL");
             fp.stall_test = stall && stall[0] == '1';
-            bool wr = false;
+            bool want_w = false, want_R = false;
             int j = i;
             while (j < n && fp.n < kMaxFrames && use_fused(fs[j], o) && fs[j].L == f.L && fs[j].K == f.K &&
                    fs[j].M == f.M) {
-                wr |= (fs[j].w != nullptr) || (fs[j].R != nullptr);
+                want_w |= fs[j].w != nullptr;
+                want_R |= fs[j].R != nullptr;
                 fp.f[fp.n++] = fs[j];
                 ++j;
             }
-            int e = launch_fused_tuned(c, fp, wr, s);
+            // R, when asked for, comes from its own covariance pass; z, P (and w)
+            // from the factorising launch
+            if (want_R) {
+                if (int e = launch_fused_tuned(c, fp, FUSED_R, s)) return e;
+            }
+            int e = launch_fused_tuned(c, fp, want_w ? FUSED_W : FUSED_ZP, s);
             if (e) return e;
             i = j;
         } else if (f.Nb > 0) {
@@ -474,7 +480,7 @@ static int get_capon_host(cos_capon_ctx *c, void *z, float *P, void *w, void *R,
     // runs whole, so the autotuner times the frame once, on one stream.
     const bool fused = use_fused(make_frame(probe, o), o);
     const bool no_scratch = fused || Nb > 0 || sliding;
-    const bool tuned = !fused || c->tuned.count(std::make_tuple(L, Yavg, M, (int)(w != nullptr || R != nullptr)));
+    const bool tuned = !fused || c->tuned.count(std::make_tuple(L, Yavg, M, (int)(w ? FUSED_W : FUSED_ZP)));
     if (no_scratch && tuned && !R && !V && Nx >= 4 && is_pinned(x) && is_pinned(z) && (!P || is_pinned(P)) &&
         (!w || is_pinned(w))) {
         if (!c->stream2 && cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking) != cudaSuccess) {

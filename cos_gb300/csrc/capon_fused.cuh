@@ -139,9 +139,9 @@ COS_DEV int unit_frame(const FramesParam &fp, long long u)
     return f;
 }
 
-// WR: the instantiation that can also write w and R; the z/P-only one omits
-// that code so its instruction footprint stays smaller.
-template <class C, bool WR>
+// MODE (FusedMode): z/P, z/P and w, or R alone; each mode carries only its
+// own output code, so its unrolled instruction stream stays small.
+template <class C, int MODE>
 __global__ void __launch_bounds__(C::WARPS * 32, 1)
 fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsigned *status)
 {
@@ -416,27 +416,30 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
                     if (q == r) A[m * G + q][m].x += dl;
 
             // ---- optional R output (loaded covariance)
-            if (WR && f.R && active) {
-                const size_t pix = (size_t)bx * f.Npy + p;
-                float2 *Rp = f.R + pix * L * L;
-                const float norm = f.r_layout == COS_CAPON_R_REFERENCE ? 1.0f : 1.0f / ((float)Ns * (float)T);
+            if (MODE == FUSED_R) {
+                if (f.R && active) {
+                    const size_t pix = (size_t)bx * f.Npy + p;
+                    float2 *Rp = f.R + pix * L * L;
+                    const float norm = f.r_layout == COS_CAPON_R_REFERENCE ? 1.0f : 1.0f / ((float)Ns * (float)T);
 #pragma unroll
-                for (int m = 0; m < NM; ++m) {
-                    const int j = m * G + r;
+                    for (int m = 0; m < NM; ++m) {
+                        const int j = m * G + r;
 #pragma unroll
-                    for (int k = 0; k < L; ++k) {
-                        if (k < m * G + G && k <= j) {
-                            const float2 v = cscale(A[k][m], norm);
-                            if (f.r_layout == COS_CAPON_R_REFERENCE) {
-                                Rp[k + (size_t)j * L] = v;
-                                if (k < j) Rp[j + (size_t)k * L] = cconj(v);
-                            } else {
-                                Rp[(size_t)k * L + j] = v;
-                                if (k < j) Rp[(size_t)j * L + k] = cconj(v);
+                        for (int k = 0; k < L; ++k) {
+                            if (k < m * G + G && k <= j) {
+                                const float2 v = cscale(A[k][m], norm);
+                                if (f.r_layout == COS_CAPON_R_REFERENCE) {
+                                    Rp[k + (size_t)j * L] = v;
+                                    if (k < j) Rp[j + (size_t)k * L] = cconj(v);
+                                } else {
+                                    Rp[(size_t)k * L + j] = v;
+                                    if (k < j) Rp[(size_t)j * L + k] = cconj(v);
+                                }
                             }
                         }
                     }
                 }
+                continue;  // this mode writes R only
             }
 
             // ---- right-hand sides: b1 = a = 1, b2 = g (rows m*G + r)
@@ -458,6 +461,7 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
             bool bad = false;
             float s11 = 0.f;
             float2 s12 = make_float2(0.f, 0.f);
+            float dinv[NM];  // FUSED_W: 1/d_i of the lane's own rows, for the back substitution
 #pragma unroll
             for (int i = 0; i < L; ++i) {
                 const int oi = i % G, mi = i / G;
@@ -483,6 +487,7 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
                 const float4 yy = rbi[L];
                 bad |= !(dv > 0.f);
                 const float rdv = __fdividef(1.f, dv);
+                if (MODE == FUSED_W && r == oi) dinv[mi] = rdv;
                 const float2 y1 = make_float2(yy.x * rdv, yy.y * rdv), y2 = make_float2(yy.z * rdv, yy.w * rdv);
                 s11 = fmaf(yy.x, y1.x, fmaf(yy.y, y1.y, s11));
                 s12 = cadd(s12, cconjmul(make_float2(yy.x, yy.y), y2));
@@ -536,7 +541,7 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
             }
             if (bad && active && r == 0) atomicOr(status, ERR_NOT_PD);
 
-            if (WR && f.w) {
+            if (MODE == FUSED_W && f.w) {
                 // back substitution (D L^H) x = b1, rows L-1 .. 0: x = R^-1 a
                 float2 xv[NM];
 #pragma unroll
@@ -552,7 +557,7 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
                     for (int o = G / 2; o; o >>= 1) part = cadd(part, shfl2_xor(part, o, G));
                     if (r == oi) {
                         const float2 num = csub(b1[mi], part);
-                        xv[mi] = cscale(num, 1.0f / A[i][mi].x);
+                        xv[mi] = cscale(num, dinv[mi]);
                     }
                 }
                 if (active) {
@@ -573,7 +578,7 @@ size_t smem_bytes(int K, int M)
     return Smem(C::TILE, K, C::M ? C::M : M, C::L, C::WARPS, C::PPW).total;
 }
 
-template <class C, bool WR>
+template <class C, int MODE>
 int launch_cfg(FramesParam fp, unsigned *status, int num_sms, cudaStream_t s)
 {
     const FrameDev &f0 = fp.f[0];
@@ -590,23 +595,28 @@ int launch_cfg(FramesParam fp, unsigned *status, int num_sms, cudaStream_t s)
     }
     Smem S(C::TILE, f0.K, C::M ? C::M : f0.M, C::L, C::WARPS, C::PPW);
     if (S.total > kFusedSmemMax) return cudaErrorNotSupported;
-    cudaError_t e = cudaFuncSetAttribute(fused_kernel<C, WR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(fused_kernel<C, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)S.total);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fused_kernel<C, WR>, C::WARPS * 32, S.total);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fused_kernel<C, MODE>, C::WARPS * 32, S.total);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorNotSupported;
     long long grid = (long long)num_sms * per_sm;
     if (grid > begin) grid = begin;
-    fused_kernel<C, WR><<<(unsigned)grid, C::WARPS * 32, S.total, s>>>(fp, begin, status);
+    fused_kernel<C, MODE><<<(unsigned)grid, C::WARPS * 32, S.total, s>>>(fp, begin, status);
     return cudaGetLastError();
 }
 
 template <class C>
-int launch_any(const FramesParam &fp, bool wr, unsigned *status, int num_sms, cudaStream_t s)
+int launch_any(const FramesParam &fp, int mode, unsigned *status, int num_sms, cudaStream_t s)
 {
-    return wr ? launch_cfg<C, true>(fp, status, num_sms, s) : launch_cfg<C, false>(fp, status, num_sms, s);
+    switch (mode) {
+    case FUSED_ZP: return launch_cfg<C, FUSED_ZP>(fp, status, num_sms, s);
+    case FUSED_W: return launch_cfg<C, FUSED_W>(fp, status, num_sms, s);
+    case FUSED_R: return launch_cfg<C, FUSED_R>(fp, status, num_sms, s);
+    default: return cudaErrorInvalidValue;
+    }
 }
 
 }  // namespace fused

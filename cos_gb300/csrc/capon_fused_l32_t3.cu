@@ -5,17 +5,17 @@
 
 namespace cgb {
 namespace {
-int launch_0(const FramesParam &fp, bool wr, unsigned *st, int n, cudaStream_t s)
+int launch_0(const FramesParam &fp, int mode, unsigned *st, int n, cudaStream_t s)
 {
-    return fused::launch_any<fused::Cfg<32, 8, 8, 2, 3, 64, true>>(fp, wr, st, n, s);
+    return fused::launch_any<fused::Cfg<32, 8, 8, 2, 3, 64, true>>(fp, mode, st, n, s);
 }
-int launch_1(const FramesParam &fp, bool wr, unsigned *st, int n, cudaStream_t s)
+int launch_1(const FramesParam &fp, int mode, unsigned *st, int n, cudaStream_t s)
 {
-    return fused::launch_any<fused::Cfg<32, 8, 8, 2, 3, 64, false>>(fp, wr, st, n, s);
+    return fused::launch_any<fused::Cfg<32, 8, 8, 2, 3, 64, false>>(fp, mode, st, n, s);
 }
-int launch_2(const FramesParam &fp, bool wr, unsigned *st, int n, cudaStream_t s)
+int launch_2(const FramesParam &fp, int mode, unsigned *st, int n, cudaStream_t s)
 {
-    return fused::launch_any<fused::Cfg<32, 8, 8, 2, 3, 0, true>>(fp, wr, st, n, s);
+    return fused::launch_any<fused::Cfg<32, 8, 8, 2, 3, 0, true>>(fp, mode, st, n, s);
 }
 
 const FusedCandidate kCand[] = {

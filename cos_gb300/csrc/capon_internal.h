@@ -82,12 +82,21 @@ int launch_lu_solve(float2 *x, const float2 *A, const float2 *b, int N, int batc
 // fused element-space path: candidate configurations per subarray length.
 // A candidate's launch fills the tiling fields of the frames itself; all
 // frames of one launch share L, K and M.
+// What one fused launch writes.  The modes are separate instantiations so that
+// the z/P kernel carries neither the back substitution nor the R stores, and
+// the w kernel not the R stores: the unrolled code of each stays small enough
+// for the instruction cache.
+enum FusedMode : int {
+    FUSED_ZP = 0,  // z and P
+    FUSED_W = 1,   // z, P and w (back substitution)
+    FUSED_R = 2,   // the loaded covariance R only (no factorisation)
+};
 struct FusedCandidate {
     const char *name;
     int L;
     int T;  // the temporal window 2K+1 the instantiation is compiled for
     int M;  // the channel count it is compiled for, 0 = any
-    int (*launch)(const FramesParam &fp, bool want_w_or_R, unsigned *status, int num_sms, cudaStream_t s);
+    int (*launch)(const FramesParam &fp, int mode, unsigned *status, int num_sms, cudaStream_t s);
     size_t (*smem)(int K, int M);  // dynamic shared memory of a launch for (K, M)
 };
 // shared memory one CTA may use; a candidate whose tile needs more for a
