@@ -240,6 +240,11 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
             float4 w0 = xr[j0], w1 = xr[j0 + 1], w2 = xr[j0 + 2];
 #pragma unroll
             for (int q = 0; q < 4; ++q) hi[q] = lo[q] = make_float2(0.f, 0.f);
+            // three chunks per iteration: enough independent work to cover the
+            // load and TwoSum latencies, without the code growth of a full
+            // unroll (which slows the unrolled per-pixel phases that follow
+            // through the instruction cache)
+#pragma unroll 3
             for (int s0 = 0; s0 < Ns; s0 += 4) {
                 float2 P[4], Q[4];
 #pragma unroll
