@@ -135,6 +135,24 @@ class Clocks:
                 "reasons": reasons}
 
 
+def mixed_roofline(ms: float, fp32_tflops: float, peaks: dict) -> dict:
+    """The mixed bound of the per-pixel work: the covariance (F_cov) at the
+    tensor-core TF32 rate, the Cholesky, solves and outputs at the FP32 rate,
+    t_roof = F_cov/P_TC + (F_chol + F_sol + F_out)/P_FP32 per pixel, and the
+    measured time's fraction of it.  P_TC is half the measured dense bf16 rate
+    (TF32 issues at half the bf16 rate)."""
+    bf16 = peaks.get("bf16_tflops")
+    if not bf16:
+        return None
+    f_cov = 8 * M * M * T + 2 * L * L * NS
+    f_rest = (4.0 / 3.0) * L ** 3 + 8 * L * L + 32 * L + 8 * M
+    p_tc = bf16 / 2.0
+    t_roof_ms = NPIX * (f_cov / (p_tc * 1e12) + f_rest / (fp32_tflops * 1e12)) * 1e3
+    return {"t_roof_ms": t_roof_ms, "t_measured_ms": ms, "frac": t_roof_ms / ms, "p_tc_tflops": p_tc,
+            "p_fp32_tflops": fp32_tflops, "f_cov_per_pixel": f_cov, "f_rest_per_pixel": f_rest,
+            "peak_source": "TF32 = half of MEASURED_PEAKS.json bf16_tflops; FP32 = SGEMM measured here"}
+
+
 def fp32_peak_tflops(torch) -> float:
     """cuBLAS FP32 SGEMM throughput (TF32 off): the measured CUDA-core FP32 peak."""
     torch.backends.cuda.matmul.allow_tf32 = False
@@ -441,6 +459,7 @@ def run_gpu(args) -> None:
         "roofline_hbm": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
                          "frac": (achieved_gbs / hbm_peak) if hbm_peak else None,
                          "bytes_per_pixel": BYTES_PER_PIXEL, "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
+        "roofline_mixed": mixed_roofline(ms, fp32, peaks),
         "clocks": clocks,
         "adjoint": adj,
         "config2": cfg2,
