@@ -468,6 +468,8 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
             float2 s12 = make_float2(0.f, 0.f);
             float dinv[NM];  // FUSED_W: 1/d_i of the lane's own rows, for the back substitution
 #pragma unroll
+            for (int m = 0; m < NM; ++m) dinv[m] = 0.f;
+#pragma unroll
             for (int i = 0; i < L; ++i) {
                 const int oi = i % G, mi = i / G;
                 // publish row i as (-Re, +Im, -Im, -Re) of A[i, j]: with the consumer's
@@ -492,7 +494,7 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
                 const float4 yy = rbi[L];
                 bad |= !(dv > 0.f);
                 const float rdv = __fdividef(1.f, dv);
-                if (MODE == FUSED_W && r == oi) dinv[mi] = rdv;
+                if (MODE == FUSED_W) dinv[mi] = (r == oi) ? rdv : dinv[mi];
                 const float2 y1 = make_float2(yy.x * rdv, yy.y * rdv), y2 = make_float2(yy.z * rdv, yy.w * rdv);
                 s11 = fmaf(yy.x, y1.x, fmaf(yy.y, y1.y, s11));
                 s12 = cadd(s12, cconjmul(make_float2(yy.x, yy.y), y2));
@@ -552,18 +554,26 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
 #pragma unroll
                 for (int m = 0; m < NM; ++m) xv[m] = make_float2(0.f, 0.f);
 #pragma unroll
+                // branch-free: every lane forms the candidate x_i and the owner
+                // of row i keeps it by a select (a divergent branch per row
+                // costs an instruction re-fetch on the serial chain)
                 for (int i = L - 1; i >= 0; --i) {
                     const int oi = i % G, mi = i / G;
                     float2 part = make_float2(0.f, 0.f);
 #pragma unroll
-                    for (int m = 0; m < NM; ++m)
-                        if (m >= mi && m * G + r > i) part = cadd(part, cmul(A[i][m], xv[m]));
+                    for (int m = 0; m < NM; ++m) {
+                        if (m < mi) continue;
+                        // slots left of the diagonal hold unused (possibly non-finite)
+                        // values: select the sum, do not multiply them by zero
+                        const bool upper = m > mi || r > oi;  // column m*G + r right of the diagonal
+                        const float2 t = cadd(part, cmul(A[i][m], xv[m]));
+                        part = make_float2(upper ? t.x : part.x, upper ? t.y : part.y);
+                    }
 #pragma unroll
                     for (int o = G / 2; o; o >>= 1) part = cadd(part, shfl2_xor(part, o, G));
-                    if (r == oi) {
-                        const float2 num = csub(b1[mi], part);
-                        xv[mi] = cscale(num, dinv[mi]);
-                    }
+                    const float2 xn = cscale(csub(b1[mi], part), dinv[mi]);
+                    const bool own = r == oi;
+                    xv[mi] = make_float2(own ? xn.x : xv[mi].x, own ? xn.y : xv[mi].y);
                 }
                 if (active) {
                     const float is11 = 1.0f / s11;
