@@ -49,9 +49,9 @@ EXEC_FLOP_PER_PIXEL = (8 * 2 * T * (L * (L + 1) // 2 - L) + 8 * NS * L + 2 * NS 
 # Algorithmic HBM bytes per pixel: the cube once (8 M Ny/(Ny-2K)) + z + P.
 BYTES_PER_PIXEL = 8 * M * NY / (NY - 2 * K) + 8 + 4
 # DRAM bytes per pixel of the fused kernel from one ncu capture (dram__bytes_read
-# + dram__bytes_write = 175.59 MB over 327,040 pixels, the 160-beam profiling
-# case), scaled to a full launch by the pixels it processes.
-TRAFFIC_PER_PIXEL = 175.59296e6 / 327040
+# + dram__bytes_write = 168.42 + 5.63 MB over 327,040 pixels, the 160-beam
+# profiling case), scaled to a full launch by the pixels it processes.
+TRAFFIC_PER_PIXEL = (168.418816e6 + 5.626368e6) / 327040
 CONFIG = {"workload": "capon-element-space M=64 L=32 K=2 [Nx=256,Ny=2048]", "M": M, "L": L, "K": K,
           "Nx": NX, "Ny": NY, "pixels_per_step": NPIX, "loading": D, "outputs": "z,P",
           "l2": "inputs larger than L2 (268 MB cube vs 126 MB L2)", "parallelism": "replicas"}
