@@ -549,31 +549,52 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
             if (bad && active && r == 0) atomicOr(status, ERR_NOT_PD);
 
             if (MODE == FUSED_W && f.w) {
-                // back substitution (D L^H) x = b1, rows L-1 .. 0: x = R^-1 a
+                // back substitution (D L^H) x = b1, x = R^-1 a, by blocks of G rows
+                // (block m: rows m*G + q, q < G), last block first.  The code of
+                // this stage runs between the factorisations of consecutive pixel
+                // groups and must stay small, or it pushes their unrolled code out
+                // of the instruction cache; so per block, through the (now idle)
+                // pivot-row buffer, rows padded to G+1 entries (no bank conflicts):
+                //   1. each lane sums its columns right of the block into the
+                //      block's G rows; the partial sums are exchanged, and lane r
+                //      adds up row m*G + r in a rolled loop;
+                //   2. the G x G diagonal block is transposed, so lane r holds
+                //      row m*G + r of it;
+                //   3. a rolled loop solves the block: lane q forms x_q, a shuffle
+                //      broadcasts it, lanes r < q take its term off their row.
+                // Slots left of the diagonal hold unused, possibly non-finite
+                // values: results are selected, never masked by a zero factor.
                 float2 xv[NM];
 #pragma unroll
                 for (int m = 0; m < NM; ++m) xv[m] = make_float2(0.f, 0.f);
+                float2 *const X = (float2 *)rb;  // G x (G+1) exchange / transpose area
 #pragma unroll
-                // branch-free: every lane forms the candidate x_i and the owner
-                // of row i keeps it by a select (a divergent branch per row
-                // costs an instruction re-fetch on the serial chain)
-                for (int i = L - 1; i >= 0; --i) {
-                    const int oi = i % G, mi = i / G;
-                    float2 part = make_float2(0.f, 0.f);
+                for (int m = NM - 1; m >= 0; --m) {
 #pragma unroll
-                    for (int m = 0; m < NM; ++m) {
-                        if (m < mi) continue;
-                        // slots left of the diagonal hold unused (possibly non-finite)
-                        // values: select the sum, do not multiply them by zero
-                        const bool upper = m > mi || r > oi;  // column m*G + r right of the diagonal
-                        const float2 t = cadd(part, cmul(A[i][m], xv[m]));
-                        part = make_float2(upper ? t.x : part.x, upper ? t.y : part.y);
+                    for (int q = 0; q < G; ++q) {
+                        float2 e = make_float2(0.f, 0.f);
+#pragma unroll
+                        for (int mm = m + 1; mm < NM; ++mm) e = cadd(e, cmul(A[m * G + q][mm], xv[mm]));
+                        X[q * (G + 1) + r] = e;
                     }
+                    __syncwarp();
+                    float2 acc = b1[m];
+#pragma unroll 1
+                    for (int l = 0; l < G; ++l) acc = csub(acc, X[r * (G + 1) + l]);
+                    __syncwarp();
 #pragma unroll
-                    for (int o = G / 2; o; o >>= 1) part = cadd(part, shfl2_xor(part, o, G));
-                    const float2 xn = cscale(csub(b1[mi], part), dinv[mi]);
-                    const bool own = r == oi;
-                    xv[mi] = make_float2(own ? xn.x : xv[mi].x, own ? xn.y : xv[mi].y);
+                    for (int q = 0; q < G; ++q) X[q * (G + 1) + r] = A[m * G + q][m];
+                    __syncwarp();
+                    float2 xm = xv[m];
+#pragma unroll 1
+                    for (int q = G - 1; q >= 0; --q) {
+                        const float2 xq = shfl2(cscale(acc, dinv[m]), q, G);
+                        if (r == q) xm = xq;
+                        const float2 t = csub(acc, cmul(X[r * (G + 1) + q], xq));
+                        acc = make_float2(r < q ? t.x : acc.x, r < q ? t.y : acc.y);
+                    }
+                    xv[m] = xm;
+                    __syncwarp();  // the area is rewritten by the next block (and r0 by the next pixel)
                 }
                 if (active) {
                     const float is11 = 1.0f / s11;
