@@ -260,6 +260,15 @@ beamspace_kernel(FrameDev f, float2 *__restrict__ Rbs)
 //            refinement step, P and z (g_bs = B g = the centre row's beam sums / Ns);
 //   phase C  (w requested) w = B^H x_bs / a_bs^H x_bs, one thread per output.
 static constexpr int kTileThreads = 256;
+// lanes sharing one range row in the per-row phase.  Each sums its share of
+// the subarrays' Y Y^H products in FP32 before the float-float reduction
+// across the lanes: with 8 or 4 lanes (longer FP32 sums) the worst power
+// error against FP64 grew 4-5x at M=128, L=64, Nb=5, so the row keeps 16.
+// A tile is sized so that its pixels plus their 2K halo rows make kTileRows
+// rows, whole passes of 256 / kRowLanes rows (66 rows took five passes, the
+// last with two rows).
+static constexpr int kRowLanes = 16;
+static constexpr int kTileRows = 64;
 
 template <int NB>
 struct BsTile {
@@ -352,13 +361,15 @@ beamspace_tile_kernel(FrameDev f, float2 *__restrict__ Rbs, int tile)
         VV[tid] = acc;
     }
 
-    // ---- phase A: per-row terms, one half-warp per row
+    // ---- phase A: per-row terms, kRowLanes lanes per row (each starts its
+    // share of the subarrays with a direct DFT, then slides)
     {
-        const int half = (tid >> 4) & 1, q = tid & 15, warp = tid >> 5;
-        const int c = (Ns + 15) / 16;
+        constexpr int RL = kRowLanes, RPW = 32 / kRowLanes;
+        const int sub = (tid & 31) / RL, q = tid % RL, warp = tid >> 5;
+        const int c = (Ns + RL - 1) / RL;
         const int s0 = q * c, s1 = min(Ns, s0 + c);
-        for (int base = 2 * warp; base < rows; base += kTileThreads / 16) {
-            const int r = base + half;
+        for (int base = RPW * warp; base < rows; base += kTileThreads / RL) {
+            const int r = base + sub;
             float2 P[NQ], Yg[NB];
             float en = 0.f;
 #pragma unroll
@@ -415,21 +426,21 @@ beamspace_tile_kernel(FrameDev f, float2 *__restrict__ Rbs, int tile)
 #pragma unroll
                 for (int e = 0; e < NQ; ++e) P[e] = cscale(P[e], 0.5f);
             }
-            // float-float reduction over the half-warp
+            // float-float reduction over the row's lanes
             float2 lo[NQ];
 #pragma unroll
             for (int e = 0; e < NQ; ++e) lo[e] = make_float2(0.f, 0.f);
 #pragma unroll
-            for (int o = 8; o; o >>= 1) {
+            for (int o = RL / 2; o; o >>= 1) {
 #pragma unroll
                 for (int e = 0; e < NQ; ++e) {
-                    const float2 oh = shfl2_xor(P[e], o, 16), ol = shfl2_xor(lo[e], o, 16);
+                    const float2 oh = shfl2_xor(P[e], o, RL), ol = shfl2_xor(lo[e], o, RL);
                     two_sum_acc(P[e], lo[e], oh);
                     lo[e] = fadd2(lo[e], ol);
                 }
 #pragma unroll
-                for (int b = 0; b < NB; ++b) Yg[b] = cadd(Yg[b], shfl2_xor(Yg[b], o, 16));
-                en += __shfl_xor_sync(0xffffffffu, en, o, 16);
+                for (int b = 0; b < NB; ++b) Yg[b] = cadd(Yg[b], shfl2_xor(Yg[b], o, RL));
+                en += __shfl_xor_sync(0xffffffffu, en, o, RL);
             }
             if (r < rows && q == 0) {
 #pragma unroll
@@ -611,7 +622,8 @@ beamspace_tile_kernel(FrameDev f, float2 *__restrict__ Rbs, int tile)
 template <int NB>
 static int launch_tile(const FrameDev &f, float2 *R_out, cudaStream_t s)
 {
-    int tile = 64;
+    // tile + 2K rows = whole passes of the per-row phase when K is small
+    int tile = kTileRows - 2 * f.K >= 16 ? kTileRows - 2 * f.K : 64;
     while (tile > 8 && BsTileSmem(tile, f.K, f.M, f.L, NB).total > 227 * 1024) tile /= 2;
     const BsTileSmem S(tile, f.K, f.M, f.L, NB);
     if (S.total > 227 * 1024) return cudaErrorNotSupported;
