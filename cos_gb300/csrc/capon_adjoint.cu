@@ -123,24 +123,6 @@ __global__ void __launch_bounds__(32 * kAdjWarps) adjoint_kernel(AdjDev a)
     if (a.gd && lane == 0 && dacc != 0.f) atomicAdd(a.gd, dacc);
 }
 
-// acc + a b and acc + conj(a) b as four fmas each (cadd of a cmul costs six)
-__device__ __forceinline__ float2 cmac4(float2 acc, float2 a, float2 b)
-{
-    acc.x = fmaf(a.x, b.x, acc.x);
-    acc.x = fmaf(-a.y, b.y, acc.x);
-    acc.y = fmaf(a.x, b.y, acc.y);
-    acc.y = fmaf(a.y, b.x, acc.y);
-    return acc;
-}
-__device__ __forceinline__ float2 cmac4_conj(float2 acc, float2 a, float2 b)
-{
-    acc.x = fmaf(a.x, b.x, acc.x);
-    acc.x = fmaf(a.y, b.y, acc.x);
-    acc.y = fmaf(a.x, b.y, acc.y);
-    acc.y = fmaf(-a.y, b.x, acc.y);
-    return acc;
-}
-
 // Blocks of the register-blocked kernel and its shared-memory row padding:
 // odd block lengths and an odd row pad spread the lanes of one load over the
 // banks (at M=64, L=32, K=2 at most 2-3 lanes share a bank pair).

@@ -21,6 +21,24 @@ COS_DEV float2 cmulc(float2 a, float2 b) { return make_float2(a.x * b.x + a.y * 
 // conj(a) * b
 COS_DEV float2 cconjmul(float2 a, float2 b) { return make_float2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x); }
 COS_DEV float cabs2(float2 a) { return a.x * a.x + a.y * a.y; }
+// acc + a b and acc + conj(a) b as four fmas each (cadd of a cmul costs six:
+// the compiler may not fuse the add into the products)
+COS_DEV float2 cmac4(float2 acc, float2 a, float2 b)
+{
+    acc.x = fmaf(a.x, b.x, acc.x);
+    acc.x = fmaf(-a.y, b.y, acc.x);
+    acc.y = fmaf(a.x, b.y, acc.y);
+    acc.y = fmaf(a.y, b.x, acc.y);
+    return acc;
+}
+COS_DEV float2 cmac4_conj(float2 acc, float2 a, float2 b)
+{
+    acc.x = fmaf(a.x, b.x, acc.x);
+    acc.x = fmaf(a.y, b.y, acc.x);
+    acc.y = fmaf(a.x, b.y, acc.y);
+    acc.y = fmaf(-a.y, b.x, acc.y);
+    return acc;
+}
 
 // ---- packed FP32x2 (Blackwell `fma.rn.f32x2`): two IEEE fmas per instruction
 COS_DEV float2 ffma2(float2 a, float2 b, float2 c)
