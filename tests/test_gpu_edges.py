@@ -78,3 +78,38 @@ def test_outputs_do_not_depend_on_the_batch(form):
         np.testing.assert_array_equal(zb[0], z[b])
         np.testing.assert_array_equal(Pb[0], P[b])
         np.testing.assert_array_equal(wb[0], w[b])
+
+
+def test_mixed_outputs_in_one_fused_group():
+    """Frames of equal (L, K, M) share one fused launch per output mode: R,
+    when any frame asks for it, comes from its own covariance pass, and z, P
+    (and w) from the factorising launch.  Each frame's outputs must equal
+    those of a call that is given that frame alone."""
+    import torch
+    from cos_gb300 import capon
+    L, K, M, Nx, Ny = 32, 2, 64, 3, 150
+    npy = Ny - 2 * K
+    xs = [torch.from_numpy(_cube(Nx, Ny, M, seed=30 + i)).cuda() for i in range(4)]
+    want = [(True, False), (False, True), (True, True), (False, False)]   # (w, R)
+
+    def make(x, w, R):
+        return capon.DeviceFrame(
+            x=x, L=L, K=K, d=0.01,
+            P=torch.empty((Nx, npy), dtype=torch.float32, device="cuda"),
+            w=torch.empty((Nx, npy, L), dtype=torch.complex64, device="cuda") if w else None,
+            R=torch.empty((Nx, npy, L, L), dtype=torch.complex64, device="cuda") if R else None)
+
+    ctx = capon.Context()
+    group = [make(x, w, R) for x, (w, R) in zip(xs, want)]
+    capon.capon_frames(group, ctx)
+    torch.cuda.synchronize()
+    for f, x, (w, R) in zip(group, xs, want):
+        alone = make(x, w, R)
+        capon.capon_frames([alone], ctx)
+        torch.cuda.synchronize()
+        assert torch.equal(alone.z, f.z) and torch.equal(alone.P, f.P)
+        if w:
+            assert torch.equal(alone.w, f.w)
+        if R:
+            assert torch.equal(alone.R, f.R)
+            assert bool(torch.isfinite(torch.view_as_real(f.R)).all())
