@@ -17,10 +17,11 @@
 //   4. diagonal loading d*tr(R)/L (getCaponC.pyx:257-262);
 //   5. right-looking Cholesky in its square-root-free form R = L D L^H
 //      (U = D^-1/2 (D L^H) is the reference's factor, matrixDecompc.pyx:19-50)
-//      in the same registers, the pivot row broadcast through shared memory,
-//      with the two right-hand sides a = 1 and g carried along, so b1 = L^-1 a
-//      and b2 = L^-1 g come out of the factorisation (the forward solve of
-//      linearSolvec.pyx:312-327, with y = D^-1/2 b);
+//      in the same registers, the pivot row broadcast through shared memory
+//      (in the z/P mode one step ahead of its use), with the two right-hand
+//      sides a = 1 and g carried along, so b1 = L^-1 a and b2 = L^-1 g come out
+//      of the factorisation (the forward solve of linearSolvec.pyx:312-327,
+//      with y = D^-1/2 b);
 //   6. outputs: a^H R^-1 a = |y1|^2, z = w^H g = y1^H y2 / |y1|^2
 //      (getCaponC.pyx:276-283), P = 1/((Ns*T) |y1|^2) for the normalised R,
 //      and, when asked, w = R^-1 a / |y1|^2 by back substitution with D L^H
