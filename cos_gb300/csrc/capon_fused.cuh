@@ -554,7 +554,9 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
                     // publish row i as (-Re, +Im, -Im, -Re) of A[i, j]: with the consumer's
                     // splats (vr, vr), (vi, vi) of its own A[i, j'] / d_i two packed fmas
                     // give A[k][j'] -= conj(A[i,k]) A[i,j'] / d_i.  Slot i holds d_i in
-                    // its first word; slot L carries (b1_i, b2_i).
+                    // its first word; slot L carries b1_i.  The w mode carries no
+                    // second right-hand side: z = x^H g / (a^H R^-1 a) follows from
+                    // the back substitution's x = R^-1 a.
                     // Step i writes buffer i&1, last read at step i-2, before the
                     // barrier that ended step i-1: one barrier per step suffices.
                     float4 *const rbi = rb + (i & 1) * (L + 1);
@@ -567,30 +569,25 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
 #pragma unroll
                     for (int m = 0; m < NM; ++m)
                         if (m >= mi) rbi[m * G + r] = nq[m];
-                    if (r == oi) rbi[L] = make_float4(b1[mi].x, b1[mi].y, b2[mi].x, b2[mi].y);
+                    if (r == oi) rbi[L] = make_float4(b1[mi].x, b1[mi].y, 0.f, 0.f);
                     __syncwarp();
                     const float dv = -rbi[i].x;
                     const float4 yy = rbi[L];
                     bad |= !(dv > 0.f);
                     const float rdv = __fdividef(1.f, dv);
                     if (MODE == FUSED_W) dinv[mi] = (r == oi) ? rdv : dinv[mi];
-                    const float2 y1 = make_float2(yy.x * rdv, yy.y * rdv), y2 = make_float2(yy.z * rdv, yy.w * rdv);
+                    const float2 y1 = make_float2(yy.x * rdv, yy.y * rdv);
                     s11 = fmaf(yy.x, y1.x, fmaf(yy.y, y1.y, s11));
-                    s12 = cadd(s12, cconjmul(make_float2(yy.x, yy.y), y2));
                     // right-hand sides, rows m*G + r > i:  b -= conj(A[i,row]) * b_i / d_i
                     // (for m > mi every row of the slot is below i; for m = mi only r > i%G)
                     {
-                        const float2 y1s = make_float2(y1.y, y1.x), y2s = make_float2(y2.y, y2.x);
+                        const float2 y1s = make_float2(y1.y, y1.x);
 #pragma unroll
                         for (int m = 0; m < NM; ++m) {
                             if (m < mi) continue;
                             const float2 n1 = make_float2(-A[i][m].x, -A[i][m].x), n2 = make_float2(-A[i][m].y, A[i][m].y);
                             const float2 t1 = ffma2(n2, y1s, ffma2(n1, y1, b1[m]));
-                            const float2 t2 = ffma2(n2, y2s, ffma2(n1, y2, b2[m]));
-                            if (m > mi || r > oi) {
-                                b1[m] = t1;
-                                b2[m] = t2;
-                            }
+                            if (m > mi || r > oi) b1[m] = t1;
                         }
                     }
                     // trailing update A[k][j] -= conj(A[i,k]) A[i,j] / d_i, i < k; slot (k,m) exists for m >= k/G
@@ -619,16 +616,16 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
                 }
             }
 
-            // ---- outputs (s11, s12 are complete on every lane)
+            // ---- outputs (s11, and in the z/P mode s12, are complete on every lane)
             const size_t pix = (size_t)bx * f.Npy + p;
             if (active && r == 0) {
                 const float is11 = 1.0f / s11;
-                f.z[pix] = make_float2(s12.x * is11, s12.y * is11);
+                if (MODE == FUSED_ZP) f.z[pix] = make_float2(s12.x * is11, s12.y * is11);
                 if (f.P) f.P[pix] = is11 / ((float)Ns * (float)T);
             }
             if (bad && active && r == 0) atomicOr(status, ERR_NOT_PD);
 
-            if (MODE == FUSED_W && f.w) {
+            if (MODE == FUSED_W) {
                 // back substitution (D L^H) x = b1, x = R^-1 a, by blocks of G rows
                 // (block m: rows m*G + q, q < G), last block first.  The code of
                 // this stage runs between the factorisations of consecutive pixel
@@ -676,8 +673,15 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
                     xv[m] = xm;
                     __syncwarp();  // the area is rewritten by the next block (and r0 by the next pixel)
                 }
-                if (active) {
-                    const float is11 = 1.0f / s11;
+                // z = w^H g = x^H g / (a^H R^-1 a), g the subarray sums of the pixel
+                float2 zp = make_float2(0.f, 0.f);
+#pragma unroll
+                for (int m = 0; m < NM; ++m) zp = cadd(zp, cconjmul(xv[m], gs[lpc * L + m * G + r]));
+#pragma unroll
+                for (int o = G / 2; o; o >>= 1) zp = cadd(zp, shfl2_xor(zp, o, G));
+                const float is11 = 1.0f / s11;
+                if (active && r == 0) f.z[pix] = cscale(zp, is11);
+                if (active && f.w) {
 #pragma unroll
                     for (int m = 0; m < NM; ++m) f.w[pix * L + m * G + r] = cscale(xv[m], is11);
                 }

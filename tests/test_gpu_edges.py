@@ -84,7 +84,9 @@ def test_mixed_outputs_in_one_fused_group():
     """Frames of equal (L, K, M) share one fused launch per output mode: R,
     when any frame asks for it, comes from its own covariance pass, and z, P
     (and w) from the factorising launch.  Each frame's outputs must equal
-    those of a call that is given that frame alone."""
+    those of a call that is given that frame alone: bit for bit, except z of
+    a frame without w, which the group's w-mode launch forms from x = R^-1 a
+    (z = x^H g / a^H R^-1 a) and a z/P launch from the carried L^-1 g."""
     import torch
     from cos_gb300 import capon
     L, K, M, Nx, Ny = 32, 2, 64, 3, 150
@@ -107,7 +109,12 @@ def test_mixed_outputs_in_one_fused_group():
         alone = make(x, w, R)
         capon.capon_frames([alone], ctx)
         torch.cuda.synchronize()
-        assert torch.equal(alone.z, f.z) and torch.equal(alone.P, f.P)
+        assert torch.equal(alone.P, f.P)
+        if w:
+            assert torch.equal(alone.z, f.z)
+        else:
+            scale = torch.sqrt(f.P)
+            assert float((torch.abs(alone.z - f.z) / scale).max()) < 1e-5
         if w:
             assert torch.equal(alone.w, f.w)
         if R:
