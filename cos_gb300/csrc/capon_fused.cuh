@@ -28,6 +28,9 @@
 //      (linearSolvec.pyx:330-346).
 // Arithmetic is FP32 with packed fma.rn.f32x2.
 #pragma once
+// the R-only mode leaves the factorisation after its R stores: in that
+// instantiation the rest of the per-pixel code is unreachable by design
+#pragma nv_diag_suppress 128
 #include "capon_common.cuh"
 #include "capon_internal.h"
 #include "../../include/cos_capon.h"
