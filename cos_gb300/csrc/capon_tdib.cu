@@ -33,7 +33,7 @@ static constexpr int kTdibMaxChunks = 8;   // hydrophones per lane: n_hydros <= 
 //     d = e / (r_t + sqrt(r_t^2 + e)),
 // and enters the sample index as d/(c dt) and the phase as fc d/c (a few
 // samples / cycles, so FP32 keeps ~1e-6 of a cycle).
-__global__ void tdib_kernel(TdibDev t)
+__global__ void __launch_bounds__(256, 4) tdib_kernel(TdibDev t)
 {
     const int lane = threadIdx.x & 31;
     const long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -85,6 +85,8 @@ __global__ void tdib_kernel(TdibDev t)
     const float ku = (float)(t.inv_c / t.dt), kc = (float)(t.fc * t.inv_c);
     const float qnan = __int_as_float(0x7fc00000);
     const int np = min(32, t.n_y - y0);
+    // two pixels per iteration: twice the channel-data gathers in flight
+#pragma unroll 2
     for (int p = 0; p < np; ++p) {
         const float a = __shfl_sync(0xffffffffu, ax_f, p), r = __shfl_sync(0xffffffffu, rt_f, p);
         const float r2 = __shfl_sync(0xffffffffu, rt2_f, p), fr = __shfl_sync(0xffffffffu, bfrac, p);
