@@ -85,8 +85,8 @@ __global__ void __launch_bounds__(256, 4) tdib_kernel(TdibDev t)
     const float ku = (float)(t.inv_c / t.dt), kc = (float)(t.fc * t.inv_c);
     const float qnan = __int_as_float(0x7fc00000);
     const int np = min(32, t.n_y - y0);
-    // two pixels per iteration: twice the channel-data gathers in flight
-#pragma unroll 2
+    // four pixels per iteration: more channel-data gathers in flight
+#pragma unroll 4
     for (int p = 0; p < np; ++p) {
         const float a = __shfl_sync(0xffffffffu, ax_f, p), r = __shfl_sync(0xffffffffu, rt_f, p);
         const float r2 = __shfl_sync(0xffffffffu, rt2_f, p), fr = __shfl_sync(0xffffffffu, bfrac, p);
