@@ -451,7 +451,8 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
                 continue;  // this mode writes R only
             }
 
-            // ---- right-hand sides: b1 = a = 1, b2 = g (rows m*G + r)
+            // ---- right-hand sides: b1 = a = 1, b2 = g (rows m*G + r); the w mode
+            // carries b1 only and forms z from the back substitution's x
             float2 b1[NM], b2[NM];
 #pragma unroll
             for (int m = 0; m < NM; ++m) {
@@ -466,7 +467,9 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
             //   A[k][j] -= conj(A[i][k]) A[i][j] / d_i,   b_k -= conj(A[i][k]) b_i / d_i,
             // so that b ends as L^-1 a, L^-1 g and, with y = D^-1/2 b,
             //   a^H R^-1 a = sum_i |b1_i|^2 / d_i,   a^H R^-1 g = sum_i conj(b1_i) b2_i / d_i,
-            // the sums every lane accumulates from the published pivots.
+            // the sums every lane accumulates from the published pivots.  Two
+            // loops follow: the z/P mode's with look-ahead, and the w mode's in
+            // the plain order.
             bool bad = false;
             float s11 = 0.f;
             float2 s12 = make_float2(0.f, 0.f);
