@@ -260,14 +260,15 @@ beamspace_kernel(FrameDev f, float2 *__restrict__ Rbs)
 //            refinement step, P and z (g_bs = B g = the centre row's beam sums / Ns);
 //   phase C  (w requested) w = B^H x_bs / a_bs^H x_bs, one thread per output.
 static constexpr int kTileThreads = 256;
-// lanes sharing one range row in the per-row phase.  Each sums its share of
-// the subarrays' Y Y^H products in FP32 before the float-float reduction
-// across the lanes: with 8 or 4 lanes (longer FP32 sums) the worst power
-// error against FP64 grew 4-5x at M=128, L=64, Nb=5, so the row keeps 16.
-// A tile is sized so that its pixels plus their 2K halo rows make kTileRows
-// rows, whole passes of 256 / kRowLanes rows (66 rows took five passes, the
-// last with two rows).
-static constexpr int kRowLanes = 16;
+// lanes sharing one range row in the per-row phase.  Each starts its share
+// of the subarrays with a direct DFT (fewer lanes: fewer of those per row)
+// and sums the Y Y^H products in two FP32 accumulators, alternate subarrays,
+// merged exactly before the float-float reduction across the lanes.  One
+// accumulator per lane at 8 lanes (sums twice as long) raised the worst power
+// error against FP64 4-5x at M=128, L=64, Nb=5; the pair keeps each FP32 sum
+// as short as with 16 lanes.  A tile is sized so that its pixels plus their
+// 2K halo rows make kTileRows rows, whole passes of 256 / kRowLanes rows.
+static constexpr int kRowLanes = 8;
 static constexpr int kTileRows = 64;
 
 template <int NB>
@@ -370,10 +371,12 @@ beamspace_tile_kernel(FrameDev f, float2 *__restrict__ Rbs, int tile)
         const int s0 = q * c, s1 = min(Ns, s0 + c);
         for (int base = RPW * warp; base < rows; base += kTileThreads / RL) {
             const int r = base + sub;
-            float2 P[NQ], Yg[NB];
+            // two FP32 accumulators, alternate subarrays: each sums at most
+            // ceil(ceil(Ns / RL) / 2) products before the exact TwoSum merge
+            float2 P[NQ], P2[NQ], Yg[NB];
             float en = 0.f;
 #pragma unroll
-            for (int e = 0; e < NQ; ++e) P[e] = make_float2(0.f, 0.f);
+            for (int e = 0; e < NQ; ++e) P[e] = P2[e] = make_float2(0.f, 0.f);
 #pragma unroll
             for (int b = 0; b < NB; ++b) Yg[b] = make_float2(0.f, 0.f);
             // forward-backward averaging: the same products over the flipped,
@@ -411,25 +414,35 @@ beamspace_tile_kernel(FrameDev f, float2 *__restrict__ Rbs, int tile)
                         }
                     }
                     if (pass == 0) en += e;
+                    const bool odd = ((s - s0) & 1) != 0;
 #pragma unroll
                     for (int i = 0; i < NB; ++i) {
                         if (pass == 0) Yg[i] = cadd(Yg[i], Y[i]);
 #pragma unroll
                         for (int j = i; j < NB; ++j) {
                             const int k = i * NB - i * (i - 1) / 2 + (j - i);
-                            P[k] = cadd(P[k], cmulc(Y[i], Y[j]));
+                            const float2 pr = cmulc(Y[i], Y[j]);
+                            if (odd) P2[k] = cadd(P2[k], pr);
+                            else P[k] = cadd(P[k], pr);
                         }
                     }
                 }
             }
-            if (f.fb) {
-#pragma unroll
-                for (int e = 0; e < NQ; ++e) P[e] = cscale(P[e], 0.5f);
-            }
-            // float-float reduction over the row's lanes
+            // merge the two accumulators exactly, then the float-float
+            // reduction over the row's lanes
             float2 lo[NQ];
 #pragma unroll
-            for (int e = 0; e < NQ; ++e) lo[e] = make_float2(0.f, 0.f);
+            for (int e = 0; e < NQ; ++e) {
+                lo[e] = make_float2(0.f, 0.f);
+                two_sum_acc(P[e], lo[e], P2[e]);
+            }
+            if (f.fb) {
+#pragma unroll
+                for (int e = 0; e < NQ; ++e) {
+                    P[e] = cscale(P[e], 0.5f);
+                    lo[e] = cscale(lo[e], 0.5f);
+                }
+            }
 #pragma unroll
             for (int o = RL / 2; o; o >>= 1) {
 #pragma unroll
