@@ -11,6 +11,8 @@
 // The general LU solver for cos_capon_solve (ISolver::solve) is here too.
 #include <string.h>
 
+#include <mutex>
+
 #include "capon_common.cuh"
 #include "capon_internal.h"
 #include "../../include/cos_capon.h"
@@ -99,8 +101,9 @@ int launch_plain_build_r(const FrameDev &f, float2 *R_out, int r_ref_layout, cud
 // pixel; R (column-major) is copied into shared memory as a row-major upper
 // factor U with U^H U = R (matrixDecompc.pyx:19-50 ordering), then
 // U^H y = 1 and U x = y (linearSolvec.pyx:312-346).  A non-positive pivot sets
-// ERR_NOT_PD in the status word and gives NaN, as the reference's complex
-// square root of a negative pivot would not be a Cholesky factor either.
+// ERR_NOT_PD in the status word (when one is given) and gives NaN, as the
+// reference's complex square root of a negative pivot would not be a Cholesky
+// factor either.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(32 * kPlainWarps)
 plain_solve_hpd_kernel(int L, long long batch, const float2 *__restrict__ Rin,
@@ -159,7 +162,7 @@ plain_solve_hpd_kernel(int L, long long batch, const float2 *__restrict__ Rin,
     (void)y;
     if (lane < L) xout[(size_t)sys * L + lane] = v0;
     if (lane + 32 < L) xout[(size_t)sys * L + lane + 32] = v1;
-    if (bad && lane == 0) atomicOr(status, ERR_NOT_PD);
+    if (bad && lane == 0 && status) atomicOr(status, ERR_NOT_PD);
 }
 
 int launch_plain_solve_hpd(const FrameDev &f, const float2 *R, float2 *Ria, unsigned *status,
@@ -305,38 +308,42 @@ int launch_lu_solve(float2 *x, const float2 *A, const float2 *b, int N, int batc
 // framework's memory pool or allocator callback, real-time loops that must
 // not reach the driver's allocator, or processes whose device memory is
 // reserved up front.  cos_capon_run_plain_noalloc runs the plain three-stage
-// pipeline with its two work buffers (per-pixel covariance and R^-1 a) and its
-// status word taken from file-scope __device__ arrays of fixed size, so it
-// allocates nothing.  Every GPU that loads this library holds these arrays
-// (about 8 MiB) until the process exits.
+// pipeline with its two work buffers (per-pixel covariance and R^-1 a) taken
+// from a file-scope __device__ array of fixed size, so it allocates nothing.
+// Every GPU that loads this library holds the array (8 MiB) until the process
+// exits.  Like the reference's solver, it reports no non-positive pivot: the
+// affected pixels' outputs are not finite.
 // ---------------------------------------------------------------------------
 #define COS_NOALLOC_SCRATCH_ELEMS (1u << 20)  // float2 elements: 8 MiB
 
 static __device__ __align__(256) float2 g_noalloc_scratch[COS_NOALLOC_SCRATCH_ELEMS];
-static __device__ __align__(256) unsigned g_noalloc_status[64];
 
 namespace {
 constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mu;
 float2 *g_scratch_ptr[kMaxDevices];
-unsigned *g_status_ptr[kMaxDevices];
 
-// Device addresses of the static arrays for the current device, looked up once
-// per device (the names are host-side stand-ins, not device addresses).
-int noalloc_setup(float2 **scratch, unsigned **status)
+// Device address of the static array on the current device (the array's name
+// is a host-side stand-in, not a device address).  Every call outside stream
+// capture looks it up afresh, so that a context re-created after
+// cudaDeviceReset gets the new address; a call during capture, when no lookup
+// may touch the module, reuses the address of the last call on that device.
+int noalloc_setup(cudaStream_t s, float2 **scratch)
 {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
-    if (!g_scratch_ptr[dev]) {
-        void *ps = nullptr, *pt = nullptr;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if ((e = cudaStreamIsCapturing(s, &cs)) != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(g_scratch_mu);
+    if (cs == cudaStreamCaptureStatusNone || !g_scratch_ptr[dev]) {
+        if (cs != cudaStreamCaptureStatusNone) return cudaErrorStreamCaptureUnsupported;
+        void *ps = nullptr;
         if ((e = cudaGetSymbolAddress(&ps, g_noalloc_scratch)) != cudaSuccess) return e;
-        if ((e = cudaGetSymbolAddress(&pt, g_noalloc_status)) != cudaSuccess) return e;
-        g_status_ptr[dev] = (unsigned *)pt;
         g_scratch_ptr[dev] = (float2 *)ps;
     }
     *scratch = g_scratch_ptr[dev];
-    *status = g_status_ptr[dev];
     return cudaSuccess;
 }
 }  // namespace
@@ -348,17 +355,16 @@ extern "C" int cos_capon_run_plain_noalloc(const cos_capon_frame *fr, void *stre
     using namespace cgb;
     if (!fr || !fr->x || !fr->z) return COS_CAPON_ERR_INVALID_VALUE;
     const int L = fr->L, K = fr->K, M = fr->M, Nx = fr->Nx, Ny = fr->Ny;
-    if (Nx < 1 || Ny < 1 || L < 1 || M < 1 || K < 0 || fr->Nb != 0 || L > M || 2 * K >= Ny)
+    if (Nx < 1 || Ny < 1 || L < 1 || M < 1 || K < 0 || fr->Nb < 0 || L > M || 2 * K >= Ny)
         return COS_CAPON_ERR_LAUNCH;
-    if (L > 64) return COS_CAPON_ERR_NOT_SUPPORTED;
+    if (fr->Nb > 0 || L > 64) return COS_CAPON_ERR_NOT_SUPPORTED;  // beamspace is not built here
     const size_t npix = (size_t)Nx * (Ny - 2 * K);
     const size_t need = npix * ((size_t)L * L + (size_t)L);
     if (need > COS_NOALLOC_SCRATCH_ELEMS) return COS_CAPON_ERR_OUT_OF_MEMORY;
-    float2 *scratch = nullptr;
-    unsigned *status = nullptr;
-    int e = noalloc_setup(&scratch, &status);
-    if (e) return e;
     cudaStream_t s = (cudaStream_t)stream;
+    float2 *scratch = nullptr;
+    int e = noalloc_setup(s, &scratch);
+    if (e) return e;
     FrameDev f;
     memset(&f, 0, sizeof(f));
     f.x = (const float2 *)fr->x;
@@ -373,10 +379,13 @@ extern "C" int cos_capon_run_plain_noalloc(const cos_capon_frame *fr, void *stre
     f.Ny = Ny;
     f.Npy = Ny - 2 * K;
     float2 *Rw = scratch, *Ria = scratch + npix * (size_t)L * L;
-    // the status word keeps the previous call's value: clear it first
-    if ((e = cudaMemsetAsync(status, 0, sizeof(unsigned), s)) != cudaSuccess) return e;
+    // every element the solve reads is written by the covariance pass first,
+    // so the previous call's contents never reach the outputs
     if ((e = launch_plain_build_r(f, Rw, 1, s))) return e;
-    if ((e = launch_plain_solve_hpd(f, Rw, Ria, status, s))) return e;
+    if ((e = launch_plain_solve_hpd(f, Rw, Ria, nullptr, s))) return e;
     if ((e = launch_plain_output(f, Ria, s))) return e;
+    // R is the caller's memory: the reference layout (per pixel column-major,
+    // loaded, not normalised), written by a second covariance pass
+    if (fr->R && (e = launch_plain_build_r(f, (float2 *)fr->R, 1, s))) return e;
     return 0;
 }

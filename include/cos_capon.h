@@ -234,12 +234,18 @@ int cos_capon_device_status(cos_capon_ctx *ctx);
  * call into the driver's allocator).  Its work buffers are a fixed file-scope
  * device array of 2^20 complex elements (8 MiB, held by every GPU that loads
  * the library until exit): frames with Nx*(Ny-2K)*(L*L+L) above that return
- * COS_CAPON_ERR_OUT_OF_MEMORY.  Element space only (Nb = 0), device pointers,
- * asynchronous on `stream` (a cudaStream_t, NULL = default stream); no
- * context, no cudaMalloc/cudaFree.  The first call on a device looks up the
- * array's device address; make that first call before any stream capture.
- * All calls share the array, so calls that overlap on the GPU (different
- * streams, or threads) race and must be serialised by the caller. */
+ * COS_CAPON_ERR_OUT_OF_MEMORY.  Element space only (Nb > 0 returns
+ * COS_CAPON_ERR_NOT_SUPPORTED), device pointers, asynchronous on `stream` (a
+ * cudaStream_t, NULL = default stream); no context, no cudaMalloc/cudaFree.
+ * P, w and R may be NULL; R, when given, is written in the reference GPU
+ * layout (COS_CAPON_R_REFERENCE).  Each call outside stream capture looks up
+ * the array's device address on the current device (so a context re-created
+ * after cudaDeviceReset is served correctly); a call during capture reuses the
+ * address of the last call on that device, so make one call before capturing,
+ * and recapture after a device reset.  All calls share the array, so calls
+ * that overlap on the GPU (different streams, or threads) race and must be
+ * serialised by the caller.  A non-positive Cholesky pivot is not reported (as
+ * in the reference's solver): those pixels' outputs are not finite. */
 int cos_capon_run_plain_noalloc(const cos_capon_frame *frame, void *stream);
 
 /* Human-readable text for a status code. */

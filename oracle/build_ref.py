@@ -45,7 +45,8 @@ import sysconfig
 from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = os.environ.get("COS_REFERENCE_ROOT", "/root/reference")
+# the reference tree: $COS_REFERENCE_ROOT, else a checkout beside this repository
+REF_ROOT = os.environ.get("COS_REFERENCE_ROOT", os.path.join(os.path.dirname(HERE), "..", "reference"))
 OUT = os.path.join(HERE, "_ref")
 SRC = os.path.join(OUT, "src")
 PKG = os.path.join(OUT, "pkg")

@@ -19,7 +19,8 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = "/root/reference"
+# the reference tree: $COS_REFERENCE_ROOT, else a checkout beside this repository
+REF = os.environ.get("COS_REFERENCE_ROOT", os.path.join(os.path.dirname(HERE), "..", "reference"))
 OUT = os.path.join(HERE, "_ref")
 SRC = os.path.join(OUT, "rtc_src")
 LIB = os.path.join(OUT, "librtc.so")

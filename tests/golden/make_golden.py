@@ -33,7 +33,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-REF = os.environ.get("COS_REFERENCE_ROOT", "/root/reference")
+# the reference tree: $COS_REFERENCE_ROOT, else a checkout beside this repository
+REF = os.environ.get("COS_REFERENCE_ROOT", os.path.join(ROOT, "..", "reference"))
 sys.path.insert(0, ROOT)
 
 # attribute name in setUp -> fixture key

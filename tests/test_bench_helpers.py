@@ -50,6 +50,14 @@ def test_mixed_roofline_arithmetic():
     assert bench.mixed_roofline(2.0, 70.0, {}) is None
 
 
+def test_headline_roofline_is_the_mixed_bound():
+    h = bench.headline_roofline(2.0, 70.0, {"bf16_tflops": 1900.0})
+    m = bench.mixed_roofline(2.0, 70.0, {"bf16_tflops": 1900.0})
+    assert h["bound"] == "tensor" and h["frac"] == pytest.approx(m["frac"])
+    assert h["achieved"] / h["peak"] == pytest.approx(h["frac"])
+    assert bench.headline_roofline(2.0, 70.0, {}) is None
+
+
 def test_workload_constants_are_config_1():
     assert (bench.M, bench.L, bench.K, bench.NX, bench.NY) == (64, 32, 2, 256, 2048)
     assert bench.NPIX == 256 * (2048 - 4) == 523264

@@ -4,11 +4,14 @@ Callers that cannot allocate device memory (code running inside another
 framework's allocator, real-time loops that must not reach the driver's
 allocator) get a variant of the plain FP32 pipeline whose work buffers live in
 a fixed file-scope device array.  This test calls it through the C ABI and
-checks its outputs against the context-based entry point on the same inputs,
-for two calls in a row with different data (the array keeps the previous
-call's contents, so stale state would show), and checks that a frame too large
-for the array is refused.  The file name sorts last so that a run that stops at
-the first failure has run every other test before this one.
+checks its outputs (z, P, w and the optional R) against the context-based
+entry point on the same inputs, for two calls in a row with different data
+(the array keeps the previous call's contents, so stale state would show).
+It also checks that a call allocates no device memory, that a call on a
+non-default stream gives the default stream's results, and that frames the
+array cannot hold or options it does not build are refused.  The file name
+sorts last so that a run that stops at the first failure has run every other
+test before this one.
 """
 import ctypes as C
 
@@ -21,9 +24,10 @@ TOL_P = 1e-6   # same kernels and arithmetic as the context path: results agree 
 TOL_Z = 1e-6
 
 
-def _frame(lib, x, z, P, w, L, K, d=0.01):
+def _frame(lib, x, z, P, w, L, K, d=0.01, R=None):
     Nx, Ny, M = x.shape
-    return lib.Frame(x.data_ptr(), z.data_ptr(), P.data_ptr(), w.data_ptr(), None, float(d), L, K, M, Nx, Ny, 0)
+    return lib.Frame(x.data_ptr(), z.data_ptr(), P.data_ptr(), w.data_ptr(),
+                     R.data_ptr() if R is not None else None, float(d), L, K, M, Nx, Ny, 0)
 
 
 def _outputs(torch, Nx, npy, L):
@@ -42,23 +46,51 @@ def test_noalloc_matches_context_path_twice():
         Nx, Ny, M = x.shape
         npy = Ny - 2 * K
         z, P, w = _outputs(torch, Nx, npy, L)
-        fr = _frame(_lib, x, z, P, w, L, K)
+        R = torch.empty((Nx, npy, L, L), dtype=torch.complex64, device="cuda")
+        fr = _frame(_lib, x, z, P, w, L, K, R=R)
         rc = _lib.lib.cos_capon_run_plain_noalloc(C.byref(fr), None)
         assert rc == 0, _lib.status_string(rc)
         torch.cuda.synchronize()
 
         ref = capon.DeviceFrame(x=x, L=L, K=K, d=0.01)
         ref.z, ref.P, ref.w = _outputs(torch, Nx, npy, L)
-        capon.capon_frames([ref], o=capon.opts(form=_lib.FORM_PLAIN))
+        ref.R = torch.empty_like(R)
+        capon.capon_frames([ref], o=capon.opts(form=_lib.FORM_PLAIN, r_layout=_lib.R_REFERENCE))
         torch.cuda.synchronize()
 
         Pn, Pr = P.cpu().numpy(), ref.P.cpu().numpy()
         zn, zr = z.cpu().numpy(), ref.z.cpu().numpy()
         wn, wr = w.cpu().numpy(), ref.w.cpu().numpy()
+        Rn, Rr = R.cpu().numpy(), ref.R.cpu().numpy()
         assert np.all(np.isfinite(Pn)) and np.all(Pn > 0), f"call {call}"
         assert np.max(np.abs(Pn - Pr) / Pr) <= TOL_P, f"call {call}"
         assert np.max(np.abs(zn - zr) / np.sqrt(Pr)) <= TOL_Z, f"call {call}"
         assert np.max(np.abs(wn - wr)) <= 1e-5 * np.max(np.abs(wr)), f"call {call}"
+        # R in the reference layout, the same covariance pass as the context path
+        assert np.max(np.abs(Rn - Rr)) <= 1e-6 * np.max(np.abs(Rr)), f"call {call}"
+
+
+def test_noalloc_allocates_nothing_and_honours_the_stream():
+    import torch
+    from cos_gb300 import _lib, synth
+
+    L, K = 16, 1
+    x = torch.from_numpy(synth.cube(160, 4, 32, [10.0], seed=31)).cuda()
+    Nx, Ny, M = x.shape
+    npy = Ny - 2 * K
+    z0, P0, w0 = _outputs(torch, Nx, npy, L)
+    z1, P1, w1 = _outputs(torch, Nx, npy, L)
+    f0 = _frame(_lib, x, z0, P0, w0, L, K)
+    f1 = _frame(_lib, x, z1, P1, w1, L, K)
+    assert _lib.lib.cos_capon_run_plain_noalloc(C.byref(f0), None) == 0   # warm-up: module and array resident
+    torch.cuda.synchronize()
+    free_before, _ = torch.cuda.mem_get_info()
+    s = torch.cuda.Stream()
+    assert _lib.lib.cos_capon_run_plain_noalloc(C.byref(f1), C.c_void_p(s.cuda_stream)) == 0
+    s.synchronize()
+    free_after, _ = torch.cuda.mem_get_info()
+    assert free_after == free_before, (free_before, free_after)
+    assert torch.equal(P0, P1) and torch.equal(z0, z1) and torch.equal(w0, w1)
 
 
 def test_noalloc_refuses_frames_beyond_its_array():
@@ -71,4 +103,9 @@ def test_noalloc_refuses_frames_beyond_its_array():
     fr = _frame(_lib, x, z, P, w, L, K)
     assert _lib.lib.cos_capon_run_plain_noalloc(C.byref(fr), None) == _lib.ERR_OUT_OF_MEMORY
     fr.L = 0
+    assert _lib.lib.cos_capon_run_plain_noalloc(C.byref(fr), None) == _lib.ERR_LAUNCH
+    fr.L, fr.Nx, fr.Ny = L, 1, 64
+    fr.Nb = 3   # beamspace is valid input, but not built in this entry point
+    assert _lib.lib.cos_capon_run_plain_noalloc(C.byref(fr), None) == _lib.ERR_NOT_SUPPORTED
+    fr.Nb = -1
     assert _lib.lib.cos_capon_run_plain_noalloc(C.byref(fr), None) == _lib.ERR_LAUNCH
