@@ -20,6 +20,7 @@ ERR_TIMEOUT = 909
 
 FORM_FUSED, FORM_PLAIN, FORM_TC_TF32, FORM_TC_BF16X3, FORM_TC_TF32X3 = 0, 1, 2, 3, 4
 FORM_SLIDING_INVERSE = 5
+FORM_TC_FUSED = 6
 LOAD_ELEMENT, LOAD_BEAMSPACE, LOAD_ABSOLUTE = 0, 1, 2
 R_REFERENCE, R_NORMALISED = 0, 1
 

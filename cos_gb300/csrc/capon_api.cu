@@ -120,9 +120,10 @@ static FrameDev make_frame(const cos_capon_frame &fr, const cos_capon_opts &o)
     return f;
 }
 
-static int candidates(int L, int K, const FusedCandidate **out)
+static int candidates(int L, int K, int form, const FusedCandidate **out)
 {
     *out = nullptr;
+    if (form == COS_CAPON_FORM_TC_FUSED) return tc_fused_candidates(out);
     const int T = 2 * K + 1;
     if (L == 16 && T == 1) return fused_candidates_l16_t1(out);
     if (L == 16 && T == 3) return fused_candidates_l16_t3(out);
@@ -133,13 +134,20 @@ static int candidates(int L, int K, const FusedCandidate **out)
     return 0;
 }
 
+// a candidate serves a frame when its compile-time L, T (and M) match
+static bool cand_fits(const FusedCandidate &c, const FrameDev &f)
+{
+    return c.L == f.L && c.T == 2 * f.K + 1 && (c.M == 0 || c.M == f.M) && c.smem(f.K, f.M) <= kFusedSmemMax;
+}
+
 static bool use_fused(const FrameDev &f, const cos_capon_opts &o)
 {
-    if (o.form != COS_CAPON_FORM_FUSED || f.Nb != 0 || o.refine || o.fb) return false;
+    if ((o.form != COS_CAPON_FORM_FUSED && o.form != COS_CAPON_FORM_TC_FUSED) || f.Nb != 0 || o.refine || o.fb)
+        return false;
     const FusedCandidate *c = nullptr;
-    const int n = candidates(f.L, f.K, &c);
+    const int n = candidates(f.L, f.K, o.form, &c);
     for (int i = 0; i < n; ++i)
-        if ((c[i].M == 0 || c[i].M == f.M) && c[i].smem(f.K, f.M) <= kFusedSmemMax) return true;
+        if (cand_fits(c[i], f)) return true;
     return false;
 }
 
@@ -149,16 +157,15 @@ static bool use_fused(const FrameDev &f, const cos_capon_opts &o)
 // that the outputs are the winner's.  COS_CAPON_FUSED_CONFIG=<name> forces a
 // candidate.  While the stream is being captured into a graph no timing is
 // possible, so an untuned shape then takes the first candidate.
-static int launch_fused_tuned(cos_capon_ctx *c, const FramesParam &fp, int mode, cudaStream_t s)
+static int launch_fused_tuned(cos_capon_ctx *c, const FramesParam &fp, int mode, int form, cudaStream_t s)
 {
     const FrameDev &f0 = fp.f[0];
     const FusedCandidate *cand = nullptr;
-    const int n = candidates(f0.L, f0.K, &cand);
+    const int n = candidates(f0.L, f0.K, form, &cand);
     std::vector<int> ok;
     for (int i = 0; i < n; ++i) {
         bool fits = true;
-        for (int q = 0; q < fp.n; ++q)
-            fits &= (cand[i].M == 0 || fp.f[q].M == cand[i].M) && cand[i].smem(fp.f[q].K, fp.f[q].M) <= kFusedSmemMax;
+        for (int q = 0; q < fp.n; ++q) fits &= cand_fits(cand[i], fp.f[q]);
         if (fits) ok.push_back(i);
     }
     if (ok.empty()) return COS_CAPON_ERR_NOT_SUPPORTED;
@@ -166,7 +173,7 @@ static int launch_fused_tuned(cos_capon_ctx *c, const FramesParam &fp, int mode,
         for (int i : ok)
             if (!strcmp(force, cand[i].name)) return cand[i].launch(fp, mode, c->d_status, c->num_sms, s);
     }
-    const auto key = std::make_tuple(f0.L, f0.K, f0.M, mode);
+    const auto key = std::make_tuple(f0.L, f0.K, f0.M, mode | (form << 8));
     auto it = c->tuned.find(key);
     if (it != c->tuned.end()) return cand[it->second].launch(fp, mode, c->d_status, c->num_sms, s);
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
@@ -273,7 +280,15 @@ static int run_tc(cos_capon_ctx *c, FrameDev f, int split, bool refine, cudaStre
 
 static int run_frames(cos_capon_ctx *c, const FrameDev *fs, int n, const cos_capon_opts &o, cudaStream_t s)
 {
-    if (o.form < COS_CAPON_FORM_FUSED || o.form > COS_CAPON_FORM_SLIDING_INVERSE) return COS_CAPON_ERR_NOT_SUPPORTED;
+    if (o.form < COS_CAPON_FORM_FUSED || o.form > COS_CAPON_FORM_TC_FUSED) return COS_CAPON_ERR_NOT_SUPPORTED;
+    if (o.form == COS_CAPON_FORM_TC_FUSED) {
+        // the tensor-core fused form: element space, z and P, shapes it is
+        // instantiated for; every frame is checked before the first launch
+        for (int k = 0; k < n; ++k) {
+            const FrameDev &f = fs[k];
+            if (f.Nb != 0 || f.fb || f.refine || f.w || f.R || !use_fused(f, o)) return COS_CAPON_ERR_NOT_SUPPORTED;
+        }
+    }
     if (o.form == COS_CAPON_FORM_SLIDING_INVERSE) {
         // every frame is checked before the first launch
         for (int k = 0; k < n; ++k) {
@@ -315,9 +330,9 @@ static int run_frames(cos_capon_ctx *c, const FrameDev *fs, int n, const cos_cap
             // R, when asked for, comes from its own covariance pass; z, P (and w)
             // from the factorising launch
             if (want_R) {
-                if (int e = launch_fused_tuned(c, fp, FUSED_R, s)) return e;
+                if (int e = launch_fused_tuned(c, fp, FUSED_R, o.form, s)) return e;
             }
-            int e = launch_fused_tuned(c, fp, want_w ? FUSED_W : FUSED_ZP, s);
+            int e = launch_fused_tuned(c, fp, want_w ? FUSED_W : FUSED_ZP, o.form, s);
             if (e) return e;
             i = j;
         } else if (f.Nb > 0) {
@@ -480,7 +495,7 @@ static int get_capon_host(cos_capon_ctx *c, void *z, float *P, void *w, void *R,
     // runs whole, so the autotuner times the frame once, on one stream.
     const bool fused = use_fused(make_frame(probe, o), o);
     const bool no_scratch = fused || Nb > 0 || sliding;
-    const bool tuned = !fused || c->tuned.count(std::make_tuple(L, Yavg, M, (int)(w ? FUSED_W : FUSED_ZP)));
+    const bool tuned = !fused || c->tuned.count(std::make_tuple(L, Yavg, M, (int)(w ? FUSED_W : FUSED_ZP) | (o.form << 8)));
     if (no_scratch && tuned && !R && !V && Nx >= 4 && is_pinned(x) && is_pinned(z) && (!P || is_pinned(P)) &&
         (!w || is_pinned(w))) {
         if (!c->stream2 && cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking) != cudaSuccess) {

@@ -108,6 +108,8 @@ int fused_candidates_l16_t5(const FusedCandidate **out);
 int fused_candidates_l32_t1(const FusedCandidate **out);
 int fused_candidates_l32_t3(const FusedCandidate **out);
 int fused_candidates_l32_t5(const FusedCandidate **out);
+// tensor-core fused kernel (capon_tcf.cu): z and P only, compile-time (L, T, M)
+int tc_fused_candidates(const FusedCandidate **out);
 // adjoint of the output power
 struct AdjDev {
     const float2 *x;   // [Nx][Ny][M]

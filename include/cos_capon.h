@@ -53,6 +53,13 @@ extern "C" {
    (COS_CAPON_LOAD_ABSOLUTE, d > 0) only; no R output, no refinement, no fb.
    A fresh build-up starts every opts.segment pixels along range.              */
 #define COS_CAPON_FORM_SLIDING_INVERSE 5
+/* Tensor-core fused form: the per-range-row Hankel Gram of the covariance on
+   tcgen05 (FP16 hi/lo split of row-scaled samples, three products, FP32
+   accumulation in TMEM), the window sum and the register Cholesky on chip in
+   one persistent kernel; R never reaches HBM.  Element space, z and P only
+   (w or R requested returns 801), shapes (L, 2K+1, M) = (32, 5, 64),
+   (32, 3, 64), (16, 3, 32).                                                  */
+#define COS_CAPON_FORM_TC_FUSED 6
 
 #define COS_CAPON_LOAD_ELEMENT   0  /* R_d = R + d*tr(R)/L*I before any beamspace transform
                                        (reference GPU default, buildR_kernel.cu:153-154)          */
