@@ -320,6 +320,17 @@ def run_gpu(args) -> None:
     # plain FP32 three-stage form (denominator), fewer steps
     ms_plain, _ = time_form(_lib.FORM_PLAIN, max(2, min(args.steps, 5)), max(1, min(args.warmup, 2)))
 
+    # the tensor-core fused form (per-row Hankel Gram on tcgen05, R on chip)
+    tcf = None
+    try:
+        ms_tcf, f_tcf = time_form(_lib.FORM_TC_FUSED, args.steps, args.warmup)
+        tcf = {"value": replicas.aggregate_rate(NPIX, ms_tcf, world), "unit": "pixels/s", "ms_per_step": ms_tcf,
+               "speedup_over_plain": ms_plain / ms_tcf, "fused_fp32_over_tc": ms_tcf / ms,
+               "precision": "FP16 hi/lo split of row-scaled samples, 3 products, FP32 accumulation; FP32 Cholesky"}
+    except Exception as exc:
+        f_tcf = None
+        tcf = {"error": str(exc)[:200]}
+
     # e2e through the host-pointer C-ABI call, pinned host buffers
     xp = torch.from_numpy(x_host).pin_memory()
     zp = torch.empty((NX, npy), dtype=torch.complex64).pin_memory()
@@ -446,6 +457,9 @@ def run_gpu(args) -> None:
     refo = oracle.capon(np.ascontiguousarray(x_host[beams]), D, L, K, want_w=False, nthreads=3)
     Pg = f.P.cpu().numpy()[beams]
     relP = np.abs(Pg - refo["P"]) / refo["P"]
+    if f_tcf is not None:
+        eT = np.abs(f_tcf.P.cpu().numpy()[beams] - refo["P"]) / refo["P"]
+        tcf["P_rel_err_max"], tcf["P_rel_err_median"] = float(eT.max()), float(np.median(eT))
 
     peaks = _peaks()
     fp32 = fp32_peak_tflops(torch)
@@ -459,6 +473,7 @@ def run_gpu(args) -> None:
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator, 8 scatterers, 20 dB)",
         "config": CONFIG,
+        "tc_fused": tcf,
         "plain": {"value": NPIX * world / (ms_plain * 1e-3), "ms_per_step": ms_plain,
                   "speedup_fused_over_plain": ms_plain / ms},
         "parity": {"P_rel_err_max": float(relP.max()), "P_rel_err_median": float(np.median(relP)),
