@@ -62,6 +62,12 @@ FILES = [
     ("framework/beamformer/capon/getCaponC.pyx", "getCaponC.pyx"),
     ("framework/lib/Complex.pxd", "Complex.pxd"),
     ("framework/lib/Complex.h", "Complex.h"),
+    # the "next" rows of the path: the all-options CPU Capon (forward-backward
+    # averaging, general subspace V), the LCA window selection, the steering
+    ("framework/beamformer/capon/getCaponAllC.pyx", "getCaponAllC.pyx"),
+    ("framework/beamformer/lca/lcac.py", "lcac.pyx"),
+    ("framework/beamformer/lca/lcacx.pyx", "lcacx.pyx"),
+    ("framework/beamformer/delay/tdibC.pyx", "tdibC.py"),
 ]
 
 # modules: (pyx relative to src, fully qualified module name)
@@ -70,13 +76,31 @@ MODULES = [
     ("framework/linalg/linearSolvec.pyx", "framework.linalg.linearSolvec"),
     ("framework/linalg/woodburyc.pyx", "framework.linalg.woodburyc"),
     ("getCaponC.pyx", "getCaponC"),
+    ("getCaponAllC.pyx", "getCaponAllC"),
+    ("lcac.pyx", "lcac"),
+    ("lcacx.pyx", "lcacx"),
 ]
+# pure-Python reference modules, shimmed copies imported as they are
+PY_MODULES = [("tdibC.py", "tdibC")]
 
 
 def _shim(dst_rel: str, text: str) -> str:
-    if dst_rel == "getCaponC.pyx":
+    """Shims applied to the staged copies (never to the reference tree):
+    numpy-2 type names, the missing framework.mynumpy (a numpy wrapper), the
+    unused GPU BuildR cimport and MKL spline import, Python 2 prints in the
+    pure-Python module."""
+    if dst_rel in ("getCaponC.pyx", "getCaponAllC.pyx", "lcac.pyx", "lcacx.pyx"):
         text = text.replace("cimport cython.array\n", "\n")
         text = re.sub(r"ctypedef\s+np\.int_t\s+ITYPE_t", "ctypedef long ITYPE_t", text)
+        text = text.replace("import framework.mynumpy as np", "import numpy as np")
+    if dst_rel == "getCaponAllC.pyx":
+        # cimported but never used on the CPU path (getCaponAllC.pyx:25)
+        text = text.replace("from framework.beamformer.capon.RealTimeCapon.BuildR cimport BuildR", "")
+    if dst_rel == "tdibC.py":
+        text = text.replace("from framework.mynumpy import pi", "from numpy import pi")
+        text = text.replace("import framework.mynumpy as np", "import numpy as np")
+        text = text.replace("from framework.lib.mkl.mklUnivariateSplineC import mklcUnivariateSplineC", "")
+        text = re.sub(r"print '([^']*)'", r"print('\1')", text)
     return text
 
 
@@ -119,8 +143,15 @@ def compile_modules() -> list[str]:
     for pkg_dir in ("framework", "framework/linalg"):
         os.makedirs(os.path.join(PKG, pkg_dir), exist_ok=True)
         open(os.path.join(PKG, pkg_dir, "__init__.py"), "w").close()
-    with ThreadPoolExecutor(max_workers=len(MODULES)) as ex:
-        return list(ex.map(lambda m: _compile_one(*m), MODULES))
+    built = []
+    for py, mod in PY_MODULES:
+        src = os.path.join(SRC, py)
+        if os.path.exists(src):
+            shutil.copy2(src, os.path.join(PKG, mod + ".py"))
+            built.append(os.path.join(PKG, mod + ".py"))
+    mods = [m for m in MODULES if os.path.exists(os.path.join(SRC, m[0][:-4] + ".cpp"))]
+    with ThreadPoolExecutor(max_workers=max(1, len(mods))) as ex:
+        return built + list(ex.map(lambda m: _compile_one(*m), mods))
 
 
 def main(argv: list[str]) -> None:

@@ -22,6 +22,14 @@ Writes
   reference's own getCaponC.getCaponCPy (z, zPow, w; complex128) for small
   cases covering K = 0, L = 1, L = M, one valid range row, and the
   (M, L, K) of the benchmark configurations.
+* ``capon_all_ref_cases.npz`` -- outputs of the reference's
+  getCaponAllC.getCaponCPy: forward-backward averaging in element space, and
+  a general subspace V through the branch that restores R's lower triangle
+  (both loading orders) and through its default solver.
+* ``lca_ref_cases.npz`` -- outputs of the reference's lcac.lca and lcacx.lca
+  for 1 x 1, all-ones column, general and weighted filters.
+* ``tdib_ref_cases.npz`` -- outputs of the reference's tdibC.tdib on seeded
+  steering geometries (some pixels beyond the time axis).
 """
 from __future__ import annotations
 
@@ -174,11 +182,116 @@ def woodbury_cases() -> dict:
     return out
 
 
+# getCaponAllC.pyx (the all-options CPU Capon), (Nx, Ny, M, L, K, d, seed):
+# forward-backward averaging in element space with its default Cholesky solver
+ALL_FB_CASES = [(2, 24, 16, 8, 1, 0.01, 30), (2, 30, 32, 16, 1, 0.01, 31), (1, 20, 24, 12, 2, 0.05, 32)]
+# a general subspace V: (Nx, Ny, M, L, K, d, Nb, seed)
+ALL_V_CASE = (2, 24, 16, 8, 1, 0.01, 4, 33)
+
+
+def _x(Nx, Ny, M, seed):
+    rng = np.random.default_rng(seed)
+    x = (rng.standard_normal((Nx, Ny, M)) + 1j * rng.standard_normal((Nx, Ny, M))).astype(np.complex64)
+    x += (4.0 * np.exp(1j * 0.7 * np.arange(M))[None, None, :]).astype(np.complex64)
+    return x
+
+
+def all_cases() -> dict:
+    """Outputs of the reference's getCaponAllC.getCaponCPy.  Its module flags
+    select the branches: doFBAvg with the default solver (SOLVE_CHOLESKY on
+    the upper triangle it builds); BEAMSPACE with a general V, once through the
+    branch that restores R's lower triangle before the transform (SOLVE_NUMPY,
+    np.linalg.solve) under both loading orders (DIAGONAL_LOADING_IN_BEAMSPACE),
+    and once through the default solver, which transforms an R whose lower
+    triangle was never filled (a reference defect, kept as a fixture)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ref  # noqa: E402
+    ref._prepare()
+    import getCaponAllC as A  # noqa: E402
+    out = {"fb_cases": np.array(ALL_FB_CASES, dtype=np.float64)}
+    for i, (Nx, Ny, M, L, K, d, seed) in enumerate(ALL_FB_CASES):
+        x = _x(Nx, Ny, M, seed)
+        z, zpow, w = A.getCaponCPy(x.astype(np.complex128), float(d), int(L), int(K), np.array([]), True, False)
+        out[f"fb_x{i}"], out[f"fb_z{i}"], out[f"fb_zpow{i}"], out[f"fb_w{i}"] = x, z, zpow, w
+    Nx, Ny, M, L, K, d, Nb, seed = ALL_V_CASE
+    x = _x(Nx, Ny, M, seed)
+    rng = np.random.default_rng(seed + 100)
+    V = (rng.standard_normal((Nb, L)) + 1j * rng.standard_normal((Nb, L))) / 4
+    out["v_case"] = np.array(ALL_V_CASE, dtype=np.float64)
+    out["v_x"], out["v_V"] = x, V
+    saved = (A.BEAMSPACE, A.SOLVE_NUMPY, A.SOLVE_CHOLESKY, A.DIAGONAL_LOADING_IN_BEAMSPACE)
+    try:
+        A.BEAMSPACE = True
+        for tag, numpy_solve, in_bs in (("full_bsload", True, True), ("full_elload", True, False),
+                                        ("upper_bsload", False, True)):
+            A.SOLVE_NUMPY, A.SOLVE_CHOLESKY, A.DIAGONAL_LOADING_IN_BEAMSPACE = numpy_solve, not numpy_solve, in_bs
+            z, zpow, w = A.getCaponCPy(x.astype(np.complex128), float(d), L, K, V, False, False)
+            out[f"v_{tag}_z"], out[f"v_{tag}_w"] = z, w[..., :Nb]   # beamspace weights, Nb of the L slots
+    finally:
+        A.BEAMSPACE, A.SOLVE_NUMPY, A.SOLVE_CHOLESKY, A.DIAGONAL_LOADING_IN_BEAMSPACE = saved
+    return out
+
+
+# LCA window selection: (Ny, Nx, Nw, seed) x filters
+LCA_SHAPES = [(20, 13, 5, 40), (16, 16, 4, 41)]
+LCA_FILTERS = [np.ones((1, 1)), np.ones((5, 1)), np.ones((3, 3)), np.array([[0.5, 1.0, 0.5]]).T,
+               np.array([[0.6, 0.9, 0.7], [1.0, 0.8, 0.5], [0.9, 1.0, 0.6], [0.7, 0.5, 1.0], [0.8, 0.6, 0.9]])]
+
+
+def lca_cases() -> dict:
+    """Outputs of the reference's lcac.lca (lcac.py) and lcacx.lca (lcacx.pyx)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ref  # noqa: E402
+    ref._prepare()
+    import lcac  # noqa: E402
+    import lcacx  # noqa: E402
+    out = {"shapes": np.array(LCA_SHAPES), "nfilters": np.array(len(LCA_FILTERS))}
+    for j, wrf in enumerate(LCA_FILTERS):
+        out[f"wrf{j}"] = wrf
+    for i, (Ny, Nx, Nw, seed) in enumerate(LCA_SHAPES):
+        rng = np.random.default_rng(seed)
+        Z = rng.standard_normal((Ny, Nx, Nw)) + 1j * rng.standard_normal((Ny, Nx, Nw))
+        out[f"Z{i}"] = Z
+        for j, wrf in enumerate(LCA_FILTERS):
+            r = lcac.lca(Z, np.asarray(wrf, float))
+            rx = lcacx.lca(Z, np.asarray(wrf, float))
+            out[f"img{i}_{j}"], out[f"win{i}_{j}"] = np.asarray(r[0]), np.asarray(r[1])
+            out[f"ximg{i}_{j}"], out[f"xwin{i}_{j}"] = np.asarray(rx[0]), np.asarray(rx[1])
+    return out
+
+
+# time-domain steering: tdib_oracle.scenario arguments
+TDIB_CASES = [dict(seed=50, n_h=6, n_s=400, n_x=3, n_y=40), dict(seed=51, n_h=16, n_s=900, n_x=4, n_y=120)]
+
+
+def tdib_cases() -> dict:
+    """Outputs of the reference's tdibC.tdib (tdibC.pyx:9-67, run as Python)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ref  # noqa: E402
+    import tdib_oracle  # noqa: E402
+    ref._prepare()
+    import tdibC  # noqa: E402
+    out = {"ncases": np.array(len(TDIB_CASES))}
+    for i, kw in enumerate(TDIB_CASES):
+        sc = tdib_oracle.scenario(**kw)
+        if i == 0:
+            sc["yarr"][:, -3:] = 400.0   # a few pixels beyond the time axis: NaN
+        for k, v in sc.items():
+            out[f"{k}{i}"] = np.asarray(v)
+        out[f"image{i}"] = tdibC.tdib(sc["mfdata"].astype(np.complex128), sc["mtaxe"], sc["x_r"], sc["D"],
+                                      sc["c"], sc["fc"], sc["xarr"], sc["yarr"])
+    return out
+
+
 def main() -> None:
     np.savez_compressed(os.path.join(HERE, "linalg_known_answers.npz"), **known_answers())
     np.savez_compressed(os.path.join(HERE, "capon_ref_cases.npz"), **ref_cases())
     np.savez_compressed(os.path.join(HERE, "woodbury_ref_cases.npz"), **woodbury_cases())
-    for f in ("linalg_known_answers.npz", "capon_ref_cases.npz", "woodbury_ref_cases.npz"):
+    np.savez_compressed(os.path.join(HERE, "capon_all_ref_cases.npz"), **all_cases())
+    np.savez_compressed(os.path.join(HERE, "lca_ref_cases.npz"), **lca_cases())
+    np.savez_compressed(os.path.join(HERE, "tdib_ref_cases.npz"), **tdib_cases())
+    for f in ("linalg_known_answers.npz", "capon_ref_cases.npz", "woodbury_ref_cases.npz",
+              "capon_all_ref_cases.npz", "lca_ref_cases.npz", "tdib_ref_cases.npz"):
         print(f, os.path.getsize(os.path.join(HERE, f)), "bytes")
 
 

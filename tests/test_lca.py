@@ -72,3 +72,58 @@ def test_cuda_lca_matches_oracle(shape, wrf):
         ok = np.ones(win.shape, bool)
         assert (win == rw).all()
     np.testing.assert_array_equal(img[ok], ri[ok])
+
+
+# ---- pinned to runs of the reference itself (tests/golden/lca_ref_cases.npz,
+# outputs of lcac.lca and lcacx.lca made by tests/golden/make_golden.py)
+
+def _gold():
+    import os
+    return np.load(os.path.join(os.path.dirname(__file__), "golden", "lca_ref_cases.npz"))
+
+
+def test_oracle_matches_reference_lcac():
+    """The oracle equals lcac.py's output on every pixel, except one located
+    difference: for an all-ones column filter (Yf x 1) lcac.py's fast path
+    (lcac.py:125-160) resets its running minimum inside the window loop of the
+    first segment and writes row Y_AVG instead of Y_MID, so its first interior
+    row Y_MID stays 0 / window 0; the oracle (and the CUDA kernel) select that
+    row like every other interior row."""
+    g = _gold()
+    for i in range(len(g["shapes"])):
+        Z = g[f"Z{i}"]
+        for j in range(int(g["nfilters"])):
+            wrf = g[f"wrf{j}"]
+            oi, ow = lca_oracle.lca(Z, wrf)[:2]
+            ri, rw = g[f"img{i}_{j}"], g[f"win{i}_{j}"]
+            ones_column = wrf.shape[1] == 1 and wrf.shape[0] > 1 and np.all(wrf == 1)
+            keep = np.ones(ow.shape, bool)
+            if ones_column:
+                ym = (wrf.shape[0] - 1) // 2
+                keep[ym] = False
+                assert np.all(ri[ym] == 0) and np.all(rw[ym] == 0)
+            np.testing.assert_array_equal(ow[keep], rw[keep])
+            np.testing.assert_array_equal(oi[keep], ri[keep])
+
+
+def test_lcacx_selects_the_transposed_neighbourhood():
+    """lcacx.pyx fills its power array as [w][x][y] and reads it as [w][y][x]
+    (lcacx.pyx:185-205): on a square image its general-filter window at pixel
+    (a, b) is the window lcac.py and the oracle choose at (b, a).  It is not
+    followed; this pins where the two modules part."""
+    g = _gold()
+    for i in range(len(g["shapes"])):
+        Z = g[f"Z{i}"]
+        if Z.shape[0] != Z.shape[1]:
+            continue
+        n = Z.shape[0]
+        for j in range(int(g["nfilters"])):
+            wrf = g[f"wrf{j}"]
+            if wrf.shape == (1, 1) or (wrf.shape[1] == 1 and np.all(wrf == 1)):
+                continue   # the 1 x 1 branch is lcac.py's; the ones-column path is covered above
+            ow = lca_oracle.lca(Z, wrf)[1]
+            xw = g[f"xwin{i}_{j}"]
+            ym, xm = (wrf.shape[0] - 1) // 2, (wrf.shape[1] - 1) // 2
+            for a in range(xm, n - xm):
+                for b in range(ym, n - ym):
+                    assert xw[a, b] == ow[b, a]

@@ -276,3 +276,93 @@ def test_sliding_inverse_rejects_invalid():
     for args in ((0.2, 4, 1, 0), (0.0, 4, 1, 3), (0.2, 9, 1, 3), (0.2, 4, 5, 3)):
         with pytest.raises(ValueError):
             oracle.capon_sliding(x, *args)
+
+
+# ---- getCaponAllC (the reference's all-options CPU Capon), pinned to runs of
+# the reference itself: tests/golden/capon_all_ref_cases.npz
+
+def _all_gold():
+    return np.load(os.path.join(os.path.dirname(__file__), "golden", "capon_all_ref_cases.npz"))
+
+
+def test_forward_backward_matches_reference_getCaponAllC():
+    """doFBAvg (getCaponAllC.pyx:346-347) with its default Cholesky solver:
+    the oracle's forward-backward averaged covariance gives the reference's z,
+    zPow and w.  The reference averages only the upper triangle it built; the
+    upper triangle of (R + J R^T J)/2 depends only on R's upper triangle, so
+    the two agree exactly."""
+    g = _all_gold()
+    for i, (Nx, Ny, M, L, K, d, _s) in enumerate(g["fb_cases"]):
+        x = g[f"fb_x{i}"]
+        o = oracle.capon(x, d, int(L), int(K), fb=True)
+        zr = g[f"fb_z{i}"]
+        np.testing.assert_allclose(o["z"], zr, rtol=0, atol=1e-11 * np.abs(zr).max())
+        np.testing.assert_allclose(o["zpow"], g[f"fb_zpow{i}"], rtol=1e-10)
+        np.testing.assert_allclose(o["w"], g[f"fb_w{i}"], rtol=0, atol=1e-11 * np.abs(g[f"fb_w{i}"]).max())
+
+
+@pytest.mark.parametrize("tag,bs_loading", [("full_bsload", True), ("full_elload", False)])
+def test_general_subspace_matches_reference_getCaponAllC(tag, bs_loading):
+    """A general V (BEAMSPACE, getCaponAllC.pyx:365-386) through the branch
+    that restores R's lower triangle before R_bs = V R V^H, loading after the
+    transform with tr(R_bs)/Nb (DIAGONAL_LOADING_IN_BEAMSPACE) or before it
+    with tr(R)/L: the oracle's z and its element-space weights V^H w_bs equal
+    the reference's."""
+    g = _all_gold()
+    Nx, Ny, M, L, K, d, Nb, _s = g["v_case"]
+    L, K, Nb = int(L), int(K), int(Nb)
+    x, V = g["v_x"], g["v_V"]
+    o = oracle.capon(x, d, L, K, Nb=Nb, V=V, bs_loading=bs_loading)
+    zr, wbs = g[f"v_{tag}_z"], g[f"v_{tag}_w"]
+    np.testing.assert_allclose(o["z"], zr, rtol=0, atol=1e-11 * np.abs(zr).max())
+    wel = np.einsum("bl,xyb->xyl", V.conj(), wbs)
+    np.testing.assert_allclose(o["w"], wel, rtol=0, atol=1e-10 * np.abs(wel).max())
+
+
+def test_reference_default_subspace_branch_uses_a_half_filled_R():
+    """The reference's default solver with a general V transforms the
+    covariance it built as an upper triangle only (its lower triangle is
+    restored only for the numpy solver, getCaponAllC.pyx:320-326), so
+    R_bs = V R_upper V^H is not Hermitian.  This restates exactly that -- the
+    upper triangle of the normalised R, the transform, loading tr(R_bs)/Nb,
+    the Cholesky with complex pivots that reads R_bs's upper triangle -- and
+    matches the
+    reference; the oracle and the GPU path use the full R instead, and differ
+    from this branch by far more than rounding."""
+    g = _all_gold()
+    Nx, Ny, M, L, K, d, Nb, _s = g["v_case"]
+    M, L, K, Nb = int(M), int(L), int(K), int(Nb)
+    x, V = g["v_x"].astype(np.complex128), g["v_V"]
+    Ns, T = M - L + 1, 2 * K + 1
+    zr = g["v_upper_bsload_z"]
+    z = np.zeros_like(zr)
+    for bx in range(x.shape[0]):
+        for p in range(x.shape[1] - 2 * K):
+            X = x[bx, p:p + T]
+            Rf = X.T.conj() @ X                                   # R_full[i,j] = sum_t conj(x_i) x_j
+            R = sum(Rf[s:s + L, s:s + L] for s in range(Ns))
+            # the upper triangle it keeps, conj * norm_inv (an FP32 scalar there, as K_inv)
+            Ru = np.triu(R.conj()) * float(np.float32(1.0 / (Ns * T)))
+            Rbs = V @ Ru @ V.conj().T
+            Rbs += np.trace(Rbs) * np.float32(d) / Nb * np.eye(Nb)
+            # its Cholesky reads the upper triangle and takes complex square
+            # roots of the (here complex) pivots (matrixDecompc.pyx:19-50),
+            # then U^H y = a, U x = y (linearSolvec.pyx:312-346)
+            U = np.zeros((Nb, Nb), complex)
+            for i in range(Nb):
+                U[i, i] = np.sqrt(Rbs[i, i] - np.sum(U[:i, i].conj() * U[:i, i]))
+                for j in range(i + 1, Nb):
+                    U[i, j] = (Rbs[i, j] - np.sum(U[:i, i].conj() * U[:i, j])) / U[i, i]
+            a = V @ np.ones(L)
+            y = np.zeros(Nb, complex)
+            for i in range(Nb):
+                y[i] = (a[i] - np.sum(U[:i, i].conj() * y[:i])) / U[i, i].conj()
+            ria = np.zeros(Nb, complex)
+            for i in reversed(range(Nb)):
+                ria[i] = (y[i] - np.sum(U[i, i + 1:] * ria[i + 1:])) / U[i, i]
+            w = ria / (a.conj() @ ria)
+            gs = V @ np.array([x[bx, p + K, i:i + Ns].sum() * float(np.float32(1.0 / Ns)) for i in range(L)])
+            z[bx, p] = np.sum(w.conj() * gs)
+    np.testing.assert_allclose(z, zr, rtol=0, atol=1e-11 * np.abs(zr).max())
+    o = oracle.capon(g["v_x"], d, L, K, Nb=Nb, V=V, bs_loading=True)
+    assert np.max(np.abs(o["z"] - zr)) > 1e-3 * np.abs(zr).max()

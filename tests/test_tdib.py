@@ -87,3 +87,20 @@ def test_steering_then_capon_matches_oracle_chain():
     relP = (np.abs(P - ref["P"]) / ref["P"]).max()
     print(f"steer -> capon P {relP:.2e}")
     assert relP < 1e-4
+
+
+def test_oracle_matches_reference_tdibC():
+    """The oracle against runs of the reference's own tdibC.tdib
+    (tdibC.pyx:9-67, executed by tests/golden/make_golden.py with its
+    numpy/print shims), NaN placement included."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "tdib_ref_cases.npz"))
+    keys = ("mfdata", "mtaxe", "x_r", "D", "c", "fc", "xarr", "yarr")
+    for i in range(int(g["ncases"])):
+        s = {k: g[f"{k}{i}"] for k in keys}
+        s["c"], s["fc"] = float(s["c"]), float(s["fc"])
+        img = tdib_oracle.tdib(**s)
+        ref = g[f"image{i}"]
+        assert np.array_equal(np.isnan(img), np.isnan(ref))
+        m = ~np.isnan(ref)
+        np.testing.assert_allclose(img[m], ref[m], rtol=1e-10, atol=1e-10 * np.abs(ref[m]).max())
