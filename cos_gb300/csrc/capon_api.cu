@@ -65,6 +65,12 @@ struct cos_capon_ctx {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     // second stream of the pipelined host-pointer call
     cudaStream_t stream2 = nullptr;
+    // auxiliary streams of a multi-frame call: launch groups that use no
+    // context scratch run concurrently, forked from and joined back to the
+    // caller's stream by events (parallel branches when the call is captured)
+    static constexpr int kAux = 3;
+    cudaStream_t aux[kAux] = {};
+    cudaEvent_t fork_ev = nullptr, join_ev[kAux] = {};
 };
 
 static const cos_capon_opts kDefaultOpts = {COS_CAPON_FORM_FUSED, COS_CAPON_LOAD_ELEMENT, COS_CAPON_R_REFERENCE, 0, 0,
@@ -309,51 +315,115 @@ static int run_frames(cos_capon_ctx *c, const FrameDev *fs, int n, const cos_cap
     if (o.fb)
         for (int k = 0; k < n; ++k)
             if (fs[k].Nb > kBeamspaceTileMaxNb) return COS_CAPON_ERR_NOT_SUPPORTED;
-    // batch consecutive fused frames with equal (L, K, M) into one launch
-    int i = 0;
-    while (i < n) {
+    // Launch groups: consecutive fused frames with equal (L, K, M) share one
+    // persistent launch; a beamspace frame is a group of its own; element-space
+    // frames without a fused instantiation run the pipelines that use the
+    // context's work buffers (R, its factor), one after another on `s`.
+    struct Group {
+        int kind;  // 0 fused, 1 beamspace, 2 scratch pipeline
+        int first, count;
+        bool want_w, want_R;
+    };
+    std::vector<Group> groups;
+    for (int i = 0; i < n;) {
         const FrameDev &f = fs[i];
         if (use_fused(f, o)) {
+            Group g{0, i, 0, false, false};
+            int j = i;
+            while (j < n && g.count < kMaxFrames && use_fused(fs[j], o) && fs[j].L == f.L && fs[j].K == f.K &&
+                   fs[j].M == f.M) {
+                g.want_w |= fs[j].w != nullptr;
+                g.want_R |= fs[j].R != nullptr;
+                ++g.count;
+                ++j;
+            }
+            groups.push_back(g);
+            i = j;
+        } else {
+            groups.push_back(Group{f.Nb > 0 ? 1 : 2, i, 1, false, false});
+            ++i;
+        }
+    }
+    auto launch_group = [&](const Group &g, cudaStream_t st) -> int {
+        const FrameDev &f = fs[g.first];
+        if (g.kind == 0) {
             FramesParam fp;
             memset(&fp, 0, sizeof(fp));
             const char *stall = getenv("COS_CAPON_TEST_STALL");
             fp.stall_test = stall && stall[0] == '1';
-            bool want_w = false, want_R = false;
-            int j = i;
-            while (j < n && fp.n < kMaxFrames && use_fused(fs[j], o) && fs[j].L == f.L && fs[j].K == f.K &&
-                   fs[j].M == f.M) {
-                want_w |= fs[j].w != nullptr;
-                want_R |= fs[j].R != nullptr;
-                fp.f[fp.n++] = fs[j];
-                ++j;
-            }
+            for (int q = 0; q < g.count; ++q) fp.f[fp.n++] = fs[g.first + q];
             // R, when asked for, comes from its own covariance pass; z, P (and w)
             // from the factorising launch
-            if (want_R) {
-                if (int e = launch_fused_tuned(c, fp, FUSED_R, o.form, s)) return e;
+            if (g.want_R) {
+                if (int e = launch_fused_tuned(c, fp, FUSED_R, o.form, st)) return e;
             }
-            int e = launch_fused_tuned(c, fp, want_w ? FUSED_W : FUSED_ZP, o.form, s);
-            if (e) return e;
-            i = j;
-        } else if (f.Nb > 0) {
-            int e = launch_beamspace(f, nullptr, s);
+            return launch_fused_tuned(c, fp, g.want_w ? FUSED_W : FUSED_ZP, o.form, st);
+        }
+        if (g.kind == 1) {
+            int e = launch_beamspace(f, nullptr, st);
             if (e) return e;
             if (f.R) {  // element-space loaded R, as the reference copies it back (Capon.cpp:253-259)
-                FrameDev g = f;
-                g.Nb = 0;
-                if ((e = launch_plain_build_r(g, f.R, f.r_layout == COS_CAPON_R_REFERENCE ? 1 : 0, s))) return e;
+                FrameDev h = f;
+                h.Nb = 0;
+                e = launch_plain_build_r(h, f.R, f.r_layout == COS_CAPON_R_REFERENCE ? 1 : 0, st);
             }
-            ++i;
-        } else {
-            // element space without a fused instantiation (or with refinement):
-            // the precise pipeline; the plain form when asked for
-            int e = is_tc_form(o.form)                          ? run_tc(c, f, o.form, o.refine != 0, s)
-                    : (o.form == COS_CAPON_FORM_PLAIN && !o.refine) ? run_plain(c, f, s)
-                                                                    : run_precise(c, f, o.refine != 0, s);
-            if (e) return e;
-            ++i;
+            return e;
+        }
+        // element space without a fused instantiation (or with refinement):
+        // the precise pipeline; the plain form when asked for
+        return is_tc_form(o.form)                              ? run_tc(c, f, o.form, o.refine != 0, st)
+               : (o.form == COS_CAPON_FORM_PLAIN && !o.refine) ? run_plain(c, f, st)
+                                                               : run_precise(c, f, o.refine != 0, st);
+    };
+    // Groups that use no context scratch (fused, beamspace) may run side by
+    // side: the first on `s`, the next ones on the auxiliary streams, forked
+    // from `s` and joined back by events, so that one kernel's tail overlaps
+    // the next one's start (captured, they become parallel graph branches).
+    // Not while an untuned fused shape is timed by the autotuner.
+    std::vector<int> free_groups, scratch_groups;
+    bool tuned_all = true;
+    for (int k = 0; k < (int)groups.size(); ++k) {
+        const Group &g = groups[k];
+        (g.kind == 2 ? scratch_groups : free_groups).push_back(k);
+        if (g.kind == 0) {
+            const FrameDev &f = fs[g.first];
+            const int mode = g.want_w ? FUSED_W : FUSED_ZP;
+            tuned_all &= c->tuned.count(std::make_tuple(f.L, f.K, f.M, mode | (o.form << 8))) != 0;
+            if (g.want_R) tuned_all &= c->tuned.count(std::make_tuple(f.L, f.K, f.M, FUSED_R | (o.form << 8))) != 0;
         }
     }
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cs) != cudaSuccess) {
+        cudaGetLastError();
+        cs = cudaStreamCaptureStatusNone;
+    }
+    const bool side_by_side = free_groups.size() > 1 && c->fork_ev &&
+                              (tuned_all || cs != cudaStreamCaptureStatusNone) &&
+                              !getenv("COS_CAPON_SERIAL_FRAMES");
+    if (!side_by_side) {
+        for (const Group &g : groups)
+            if (int e = launch_group(g, s)) return e;
+        return 0;
+    }
+    const int naux = std::min((int)free_groups.size() - 1, cos_capon_ctx::kAux);
+    cudaError_t ce = cudaEventRecord(c->fork_ev, s);
+    for (int k = 0; k < naux && ce == cudaSuccess; ++k) ce = cudaStreamWaitEvent(c->aux[k], c->fork_ev, 0);
+    if (ce != cudaSuccess) return ce;
+    int err = 0;
+    for (int q = 0; q < (int)free_groups.size() && !err; ++q) {
+        // group 0 and the ones past the auxiliary streams on `s`
+        const cudaStream_t st = (q >= 1 && q <= naux) ? c->aux[q - 1] : s;
+        err = launch_group(groups[free_groups[q]], st);
+    }
+    // join every auxiliary stream back into `s`, also after an error
+    for (int k = 0; k < naux; ++k) {
+        cudaError_t je = cudaEventRecord(c->join_ev[k], c->aux[k]);
+        if (je == cudaSuccess) je = cudaStreamWaitEvent(s, c->join_ev[k], 0);
+        if (je != cudaSuccess && !err) err = je;
+    }
+    if (err) return err;
+    for (int k : scratch_groups)
+        if (int e = launch_group(groups[k], s)) return e;
     return 0;
 }
 
@@ -396,10 +466,20 @@ int cos_capon_create(cos_capon_ctx **ctx)
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_status, sizeof(unsigned));
     if (e == cudaSuccess) e = cudaMemset(c->d_status, 0, sizeof(unsigned));
+    for (int k = 0; k < cos_capon_ctx::kAux && e == cudaSuccess; ++k) {
+        e = cudaStreamCreateWithFlags(&c->aux[k], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->join_ev[k], cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         cudaGetLastError();
         if (c->stream) cudaStreamDestroy(c->stream);
         if (c->d_status) cudaFree(c->d_status);
+        for (int k = 0; k < cos_capon_ctx::kAux; ++k) {
+            if (c->aux[k]) cudaStreamDestroy(c->aux[k]);
+            if (c->join_ev[k]) cudaEventDestroy(c->join_ev[k]);
+        }
+        if (c->fork_ev) cudaEventDestroy(c->fork_ev);
         delete c;
         return e;
     }
@@ -419,6 +499,11 @@ int cos_capon_destroy(cos_capon_ctx *c)
     if (c->stream2) cudaStreamDestroy(c->stream2);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
+    for (int k = 0; k < cos_capon_ctx::kAux; ++k) {
+        if (c->aux[k]) cudaStreamDestroy(c->aux[k]);
+        if (c->join_ev[k]) cudaEventDestroy(c->join_ev[k]);
+    }
+    if (c->fork_ev) cudaEventDestroy(c->fork_ev);
     delete c;
     return 0;
 }
