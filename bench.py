@@ -562,8 +562,12 @@ def sliding_inverse_study(ctx, stream, xt, x_host) -> dict:
 
 PRECISION_FORMS = [  # name, form, refine
     ("all_fp32", 1, 0),                       # plain FP32 pipeline, the reference GPU algorithm
-    ("ff_cov_fp32_chol", 0, 0),               # float-float covariance, FP32 Cholesky
-    ("ff_cov_fp32_chol_fp64_refine", 1, 1),   # ... plus one FP64-residual refinement step
+    # fused kernel (L = 64: one warp per pixel, registers): float-float
+    # covariance, FP32 Cholesky; then with one FP64-residual refinement step
+    ("fused_ff_cov_fp32_chol", 0, 0),
+    ("fused_ff_cov_fp32_chol_fp64_refine", 0, 1),
+    # the same arithmetic with R materialised per pixel (precise pipeline)
+    ("precise_ff_cov_fp32_chol_fp64_refine", 1, 1),
     ("tc_tf32", 2, 0), ("tc_tf32_refine", 2, 1),
     ("tc_bf16x3", 3, 0), ("tc_bf16x3_refine", 3, 1),
     ("tc_tf32x3", 4, 0), ("tc_tf32x3_refine", 4, 1),

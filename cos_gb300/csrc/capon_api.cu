@@ -55,6 +55,8 @@ struct cos_capon_ctx {
     DevBuf x, z, P, w, R;
     // plain / precise pipeline scratch
     DevBuf Rwork, Rlo, dl, Ria;
+    // float-float covariance slots of the fused refinement mode (L > 32)
+    DevBuf stash;
     // stage entry points
     DevBuf A, b, sol;
     DevBuf V;           // subspace matrix of the host-pointer subspace call
@@ -137,6 +139,8 @@ static int candidates(int L, int K, int form, const FusedCandidate **out)
     if (L == 32 && T == 1) return fused_candidates_l32_t1(out);
     if (L == 32 && T == 3) return fused_candidates_l32_t3(out);
     if (L == 32 && T == 5) return fused_candidates_l32_t5(out);
+    if (L == 48 && T == 3) return fused_candidates_l48_t3(out);
+    if (L == 64 && T == 9) return fused_candidates_l64_t9(out);
     return 0;
 }
 
@@ -146,10 +150,17 @@ static bool cand_fits(const FusedCandidate &c, const FrameDev &f)
     return c.L == f.L && c.T == 2 * f.K + 1 && (c.M == 0 || c.M == f.M) && c.smem(f.K, f.M) <= kFusedSmemMax;
 }
 
+// the fused kernels for L > 32 carry the refinement step themselves; for
+// L <= 32 it runs in the precise pipeline
+static bool refine_in_fused(const FrameDev &f, const cos_capon_opts &o)
+{
+    return o.form == COS_CAPON_FORM_FUSED && f.L > 32;
+}
+
 static bool use_fused(const FrameDev &f, const cos_capon_opts &o)
 {
-    if ((o.form != COS_CAPON_FORM_FUSED && o.form != COS_CAPON_FORM_TC_FUSED) || f.Nb != 0 || o.refine || o.fb)
-        return false;
+    if ((o.form != COS_CAPON_FORM_FUSED && o.form != COS_CAPON_FORM_TC_FUSED) || f.Nb != 0 || o.fb) return false;
+    if (o.refine && !refine_in_fused(f, o)) return false;
     const FusedCandidate *c = nullptr;
     const int n = candidates(f.L, f.K, o.form, &c);
     for (int i = 0; i < n; ++i)
@@ -323,12 +334,14 @@ static int run_frames(cos_capon_ctx *c, const FrameDev *fs, int n, const cos_cap
         int kind;  // 0 fused, 1 beamspace, 2 scratch pipeline
         int first, count;
         bool want_w, want_R;
+        bool scratch;  // uses context scratch (the scratch pipelines, the fused refinement mode)
+        int mode() const { return scratch ? FUSED_REFINE : want_w ? FUSED_W : FUSED_ZP; }
     };
     std::vector<Group> groups;
     for (int i = 0; i < n;) {
         const FrameDev &f = fs[i];
         if (use_fused(f, o)) {
-            Group g{0, i, 0, false, false};
+            Group g{0, i, 0, false, false, o.refine != 0};
             int j = i;
             while (j < n && g.count < kMaxFrames && use_fused(fs[j], o) && fs[j].L == f.L && fs[j].K == f.K &&
                    fs[j].M == f.M) {
@@ -340,7 +353,7 @@ static int run_frames(cos_capon_ctx *c, const FrameDev *fs, int n, const cos_cap
             groups.push_back(g);
             i = j;
         } else {
-            groups.push_back(Group{f.Nb > 0 ? 1 : 2, i, 1, false, false});
+            groups.push_back(Group{f.Nb > 0 ? 1 : 2, i, 1, false, false, f.Nb == 0});
             ++i;
         }
     }
@@ -357,7 +370,19 @@ static int run_frames(cos_capon_ctx *c, const FrameDev *fs, int n, const cos_cap
             if (g.want_R) {
                 if (int e = launch_fused_tuned(c, fp, FUSED_R, o.form, st)) return e;
             }
-            return launch_fused_tuned(c, fp, g.want_w ? FUSED_W : FUSED_ZP, o.form, st);
+            if (g.scratch) {
+                // the stash for the largest candidate of the shape
+                const FusedCandidate *cand = nullptr;
+                const int nc = candidates(f.L, f.K, o.form, &cand);
+                size_t need = 0;
+                for (int q = 0; q < nc; ++q)
+                    if (cand[q].stash && cand_fits(cand[q], f)) need = std::max(need, cand[q].stash(c->num_sms));
+                if (need == 0) return COS_CAPON_ERR_NOT_SUPPORTED;
+                if (int e = c->stash.ensure(need)) return e;
+                fp.stash = (float4 *)c->stash.p;
+                fp.stash_bytes = c->stash.cap;
+            }
+            return launch_fused_tuned(c, fp, g.mode(), o.form, st);
         }
         if (g.kind == 1) {
             int e = launch_beamspace(f, nullptr, st);
@@ -384,10 +409,10 @@ static int run_frames(cos_capon_ctx *c, const FrameDev *fs, int n, const cos_cap
     bool tuned_all = true;
     for (int k = 0; k < (int)groups.size(); ++k) {
         const Group &g = groups[k];
-        (g.kind == 2 ? scratch_groups : free_groups).push_back(k);
+        (g.scratch ? scratch_groups : free_groups).push_back(k);
         if (g.kind == 0) {
             const FrameDev &f = fs[g.first];
-            const int mode = g.want_w ? FUSED_W : FUSED_ZP;
+            const int mode = g.mode();
             tuned_all &= c->tuned.count(std::make_tuple(f.L, f.K, f.M, mode | (o.form << 8))) != 0;
             if (g.want_R) tuned_all &= c->tuned.count(std::make_tuple(f.L, f.K, f.M, FUSED_R | (o.form << 8))) != 0;
         }
@@ -491,8 +516,8 @@ int cos_capon_destroy(cos_capon_ctx *c)
 {
     if (!c) return COS_CAPON_ERR_INVALID_VALUE;
     cudaStreamSynchronize(c->stream);
-    for (DevBuf *b : {&c->x, &c->z, &c->P, &c->w, &c->R, &c->Rwork, &c->Rlo, &c->dl, &c->Ria, &c->A, &c->b,
-                      &c->sol, &c->V, &c->tdib_in, &c->lca_pw})
+    for (DevBuf *b : {&c->x, &c->z, &c->P, &c->w, &c->R, &c->Rwork, &c->Rlo, &c->dl, &c->Ria, &c->stash, &c->A,
+                      &c->b, &c->sol, &c->V, &c->tdib_in, &c->lca_pw})
         b->release();
     if (c->d_status) cudaFree(c->d_status);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -579,7 +604,7 @@ static int get_capon_host(cos_capon_ctx *c, void *z, float *P, void *w, void *R,
     // chunk overlap the kernel of the other.  The first call of a fused shape
     // runs whole, so the autotuner times the frame once, on one stream.
     const bool fused = use_fused(make_frame(probe, o), o);
-    const bool no_scratch = fused || Nb > 0 || sliding;
+    const bool no_scratch = (fused && !o.refine) || Nb > 0 || sliding;
     const bool tuned = !fused || c->tuned.count(std::make_tuple(L, Yavg, M, (int)(w ? FUSED_W : FUSED_ZP) | (o.form << 8)));
     if (no_scratch && tuned && !R && !V && Nx >= 4 && is_pinned(x) && is_pinned(z) && (!P || is_pinned(P)) &&
         (!w || is_pinned(w))) {

@@ -32,6 +32,7 @@
 // instantiation the rest of the per-pixel code is unreachable by design
 #pragma nv_diag_suppress 128
 #include "capon_common.cuh"
+#include "capon_fused_wide.cuh"
 #include "capon_internal.h"
 #include "../../include/cos_capon.h"
 
@@ -112,6 +113,13 @@ struct Cfg {
     static constexpr int NM = L / G;       // column slots per lane
     static constexpr int PPW = 32 / G;     // pixels per warp
     static constexpr int TILE = WARPS * PPW * NITER;
+    // L > 32: the blocked per-pixel path of capon_fused_wide.cuh
+    static constexpr bool WIDE = L > 32;
+    // float4 slots of a pixel group's shared area: the pivot-row buffers (and,
+    // wide, the first covariance row and the 1/d of factored rows), or the
+    // G x (G+1) exchange area of the w mode's back substitution
+    static constexpr int AREA = WIDE ? WideArea<L, G>::Q : 2 * (L + 1);
+    static constexpr int RBQ = AREA > (G * (G + 1) + 1) / 2 ? AREA : (G * (G + 1) + 1) / 2;
     static_assert(L % G == 0 && 32 % G == 0, "G must divide L and 32");
 };
 
@@ -119,7 +127,7 @@ struct Cfg {
 struct Smem {
     int rows, XS;  // tile rows (TILE+2K), expanded row stride (quads)
     size_t off_raw0, off_raw1, off_xe, off_c, off_g, off_rb, off_bar, total;
-    __host__ __device__ Smem(int TILE, int K, int M, int L, int WARPS, int PPW)
+    __host__ __device__ Smem(int TILE, int K, int M, int L, int WARPS, int PPW, int RBQ)
     {
         rows = TILE + 2 * K;
         XS = M + 2;
@@ -130,7 +138,7 @@ struct Smem {
         off_c = off_xe + (((size_t)rows * XS * sizeof(float4) + 127) & ~(size_t)127);
         off_g = off_c + (((size_t)2 * rows * L * sizeof(float2) + 127) & ~(size_t)127);
         off_rb = off_g + (((size_t)TILE * L * sizeof(float2) + 127) & ~(size_t)127);
-        off_bar = off_rb + (((size_t)2 * WARPS * PPW * (L + 1) * sizeof(float4) + 127) & ~(size_t)127);
+        off_bar = off_rb + (((size_t)WARPS * PPW * RBQ * sizeof(float4) + 127) & ~(size_t)127);
         total = off_bar + 64;
     }
 };
@@ -158,14 +166,14 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
     // all frames of one launch share K and M bounds through the first frame's
     // carve-up; the host groups frames so that K and M are equal within a launch
     const FrameDev &f0 = fp.f[0];
-    const Smem S(TILE, K, C::M ? C::M : f0.M, L, C::WARPS, PPW);
+    const Smem S(TILE, K, C::M ? C::M : f0.M, L, C::WARPS, PPW, C::RBQ);
     float2 *raw[2] = {(float2 *)(smem + S.off_raw0), (float2 *)(smem + S.off_raw1)};
     float4 *xe = (float4 *)(smem + S.off_xe);
     float2 *cs = (float2 *)(smem + S.off_c);
     float2 *cl = cs + (size_t)S.rows * L;
     float2 *gs = (float2 *)(smem + S.off_g);
     // two pivot-row buffers per pixel group, alternating by Cholesky step
-    float4 *rb = (float4 *)(smem + S.off_rb) + (size_t)(warp * PPW + gi) * 2 * (L + 1);
+    float4 *rb = (float4 *)(smem + S.off_rb) + (size_t)(warp * PPW + gi) * C::RBQ;
     uint64_t *bar = (uint64_t *)(smem + S.off_bar);
 
     if (tid == 0) {
@@ -244,6 +252,32 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
             float4 w0 = xr[j0], w1 = xr[j0 + 1], w2 = xr[j0 + 2];
 #pragma unroll
             for (int q = 0; q < 4; ++q) hi[q] = lo[q] = make_float2(0.f, 0.f);
+            if constexpr (MODE == FUSED_REFINE) {
+                // the refinement mode: exact products (TwoProd by fma) and
+                // float-float sums.  The recurrence carries this row into every
+                // diagonal of R, so its rounding would be the same along a whole
+                // diagonal, an error the refinement's residual would keep.
+#pragma unroll 2
+                for (int s = 0; s < Ns; ++s) {
+                    const float4 a = xr[s], w3 = xr[s + j0 + 3];
+                    const float4 c[4] = {w0, w1, w2, w3};
+                    const float2 an = make_float2(a.x, a.y), az = make_float2(a.z, a.w);
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        // a conj(c) = c.re (ar, ai) + c.im (ai, -ar)
+                        const float2 sr = make_float2(c[q].x, c[q].x), si = make_float2(c[q].y, c[q].y);
+                        const float2 p1 = fmul2(sr, an), p2 = fmul2(si, az);
+                        const float2 e = fadd2(ffma2(sr, an, make_float2(-p1.x, -p1.y)),
+                                               ffma2(si, az, make_float2(-p2.x, -p2.y)));
+                        two_sum_acc(hi[q], lo[q], p1);
+                        two_sum_acc(hi[q], lo[q], p2);
+                        lo[q] = fadd2(lo[q], e);
+                    }
+                    w0 = w1;
+                    w1 = w2;
+                    w2 = w3;
+                }
+            } else {
             // three chunks per iteration: enough independent work to cover the
             // load and TwoSum latencies, without the code growth of a full
             // unroll (which slows the unrolled per-pixel phases that follow
@@ -272,6 +306,7 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
                 }
 #pragma unroll
                 for (int q = 0; q < 4; ++q) two_sum_acc(hi[q], lo[q], make_float2(P[q].x + P[q].y, Q[q].x + Q[q].y));
+            }
             }
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
@@ -319,6 +354,15 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
             const int lpc = lp;  // rows lp..lp+2K lie inside the TILE+2K row buffers; past `rows` they are stale
             const float4 *xw = xe + (size_t)lpc * XS;
 
+            if constexpr (C::WIDE) {
+                float4 *const stash =
+                    MODE == FUSED_REFINE
+                        ? fp.stash + ((size_t)blockIdx.x * C::WARPS * PPW + warp * PPW + gi) * WideStash<L, G>::Q
+                        : nullptr;
+                wide_pixel<C, MODE>(f, xw, XS, Ns, cs + (size_t)lpc * L, cl + (size_t)lpc * L, gs + (size_t)lpc * L, rb,
+                                    stash, r, active, (size_t)bx * f.Npy + p, status);
+                continue;
+            }
             float2 A[L][NM];
             // First covariance row R0[d] = sum_t c_{y+t}[d] (float-float, rounded once),
             // shared by the group through shared memory.
@@ -701,7 +745,24 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
 template <class C>
 size_t smem_bytes(int K, int M)
 {
-    return Smem(C::TILE, K, C::M ? C::M : M, C::L, C::WARPS, C::PPW).total;
+    return Smem(C::TILE, K, C::M ? C::M : M, C::L, C::WARPS, C::PPW, C::RBQ).total;
+}
+
+// bytes of FramesParam::stash the refinement mode needs on num_sms SMs
+template <class C>
+size_t stash_bytes(int num_sms)
+{
+    if constexpr (!C::WIDE) {
+        return 0;
+    } else {
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fused_kernel<C, FUSED_REFINE>, C::WARPS * 32, 0) !=
+            cudaSuccess) {
+            cudaGetLastError();
+            return 0;
+        }
+        return (size_t)num_sms * per_sm * C::WARPS * C::PPW * WideStash<C::L, C::G>::Q * sizeof(float4);
+    }
 }
 
 template <class C, int MODE>
@@ -719,7 +780,7 @@ int launch_cfg(FramesParam fp, unsigned *status, int num_sms, cudaStream_t s)
         g.tile_begin = begin;
         begin += (long long)g.Nx * g.tiles_per_beam;
     }
-    Smem S(C::TILE, f0.K, C::M ? C::M : f0.M, C::L, C::WARPS, C::PPW);
+    Smem S(C::TILE, f0.K, C::M ? C::M : f0.M, C::L, C::WARPS, C::PPW, C::RBQ);
     if (S.total > kFusedSmemMax) return cudaErrorNotSupported;
     cudaError_t e = cudaFuncSetAttribute(fused_kernel<C, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)S.total);
@@ -730,6 +791,9 @@ int launch_cfg(FramesParam fp, unsigned *status, int num_sms, cudaStream_t s)
     if (per_sm < 1) return cudaErrorNotSupported;
     long long grid = (long long)num_sms * per_sm;
     if (grid > begin) grid = begin;
+    if (MODE == FUSED_REFINE &&
+        (!fp.stash || fp.stash_bytes < (size_t)grid * C::WARPS * C::PPW * WideStash<C::L, C::G>::Q * sizeof(float4)))
+        return cudaErrorNotSupported;
     fused_kernel<C, MODE><<<(unsigned)grid, C::WARPS * 32, S.total, s>>>(fp, begin, status);
     return cudaGetLastError();
 }
@@ -741,6 +805,9 @@ int launch_any(const FramesParam &fp, int mode, unsigned *status, int num_sms, c
     case FUSED_ZP: return launch_cfg<C, FUSED_ZP>(fp, status, num_sms, s);
     case FUSED_W: return launch_cfg<C, FUSED_W>(fp, status, num_sms, s);
     case FUSED_R: return launch_cfg<C, FUSED_R>(fp, status, num_sms, s);
+    case FUSED_REFINE:
+        if constexpr (C::WIDE) return launch_cfg<C, FUSED_REFINE>(fp, status, num_sms, s);
+        return cudaErrorNotSupported;
     default: return cudaErrorInvalidValue;
     }
 }

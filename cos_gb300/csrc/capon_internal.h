@@ -35,6 +35,10 @@ struct FramesParam {
     // bounded wait runs out and the launch reports ERR_TIMEOUT (the test of
     // the timeout path; set from COS_CAPON_TEST_STALL, never by default)
     int stall_test;
+    // FUSED_REFINE: per pixel group, the float-float covariance slots kept for
+    // the residual (fused::WideStash); indexed by the launch's group number
+    float4 *stash;
+    size_t stash_bytes;
 };
 
 // Error bits written to the device status word.
@@ -90,6 +94,7 @@ enum FusedMode : int {
     FUSED_ZP = 0,  // z and P
     FUSED_W = 1,   // z, P and w (back substitution)
     FUSED_R = 2,   // the loaded covariance R only (no factorisation)
+    FUSED_REFINE = 3,  // z, P (and w) with one refinement step of R^-1 a (L > 32)
 };
 struct FusedCandidate {
     const char *name;
@@ -98,6 +103,8 @@ struct FusedCandidate {
     int M;  // the channel count it is compiled for, 0 = any
     int (*launch)(const FramesParam &fp, int mode, unsigned *status, int num_sms, cudaStream_t s);
     size_t (*smem)(int K, int M);  // dynamic shared memory of a launch for (K, M)
+    // FUSED_REFINE: bytes of FramesParam::stash a launch needs (0: no refinement mode)
+    size_t (*stash)(int num_sms);
 };
 // shared memory one CTA may use; a candidate whose tile needs more for a
 // frame's (K, M) is not used for it (the precise pipeline takes the frame)
@@ -108,6 +115,8 @@ int fused_candidates_l16_t5(const FusedCandidate **out);
 int fused_candidates_l32_t1(const FusedCandidate **out);
 int fused_candidates_l32_t3(const FusedCandidate **out);
 int fused_candidates_l32_t5(const FusedCandidate **out);
+int fused_candidates_l48_t3(const FusedCandidate **out);
+int fused_candidates_l64_t9(const FusedCandidate **out);
 // tensor-core fused kernel (capon_tcf.cu): z and P only, compile-time (L, T, M)
 int tc_fused_candidates(const FusedCandidate **out);
 // adjoint of the output power

@@ -366,3 +366,28 @@ def test_reference_default_subspace_branch_uses_a_half_filled_R():
     np.testing.assert_allclose(z, zr, rtol=0, atol=1e-11 * np.abs(zr).max())
     o = oracle.capon(g["v_x"], d, L, K, Nb=Nb, V=V, bs_loading=True)
     assert np.max(np.abs(o["z"] - zr)) > 1e-3 * np.abs(zr).max()
+
+
+def test_fp32_factorisation_limit_on_the_precision_stress_case():
+    """What FP32 arithmetic can reach on the config-3 stress data (two coherent
+    scatterers one beam apart at 40 dB, loading 1e-3, L=64, K=4), with the
+    oracle's FP64 R as input: rounded once to complex64 and factored by
+    single-precision LAPACK, the output power misses 1e-4 on the most
+    ill-conditioned pixels (cond ~3e4); one refinement step with an FP64
+    residual against the exact R brings every pixel within 1e-6.  The GPU
+    kernels' bars for this data (tests/test_gpu_wide.py) follow from it."""
+    import scipy.linalg as sl
+    from cos_gb300 import synth
+    x = synth.cube(200, 3, 128, [100.0, 100.0], seed=3, coherent_pair=True)
+    x = np.ascontiguousarray(x[2:, 60:120])   # the pair's beam, the scatterers' range
+    o = oracle.capon(x, 1e-3, 64, 4, want_w=False, want_R=True, nthreads=os.cpu_count() or 1)
+    a = np.ones(64)
+    e0, e1 = [], []
+    for R, P in zip(o["R"].reshape(-1, 64, 64), o["P"].ravel()):
+        c = sl.cho_factor(R.astype(np.complex64))
+        x0 = sl.cho_solve(c, a.astype(np.complex64)).astype(np.complex128)
+        x1 = x0 + sl.cho_solve(c, (a - R @ x0).astype(np.complex64))
+        e0.append(abs(1 / np.real(a @ x0) - P) / P)
+        e1.append(abs(1 / np.real(a @ x1) - P) / P)
+    assert max(e0) > 1e-4
+    assert max(e1) < 1e-6
