@@ -23,6 +23,7 @@ FORM_SLIDING_INVERSE = 5
 FORM_TC_FUSED = 6
 LOAD_ELEMENT, LOAD_BEAMSPACE, LOAD_ABSOLUTE = 0, 1, 2
 R_REFERENCE, R_NORMALISED = 0, 1
+REFINE_NONE, REFINE_ALL, REFINE_ADAPTIVE = 0, 1, 2
 
 # every symbol include/cos_capon.h declares
 EXPORTS = (

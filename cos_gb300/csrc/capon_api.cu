@@ -334,14 +334,19 @@ static int run_frames(cos_capon_ctx *c, const FrameDev *fs, int n, const cos_cap
         int kind;  // 0 fused, 1 beamspace, 2 scratch pipeline
         int first, count;
         bool want_w, want_R;
-        bool scratch;  // uses context scratch (the scratch pipelines, the fused refinement mode)
-        int mode() const { return scratch ? FUSED_REFINE : want_w ? FUSED_W : FUSED_ZP; }
+        bool scratch;  // uses context scratch (the scratch pipelines, the fused refinement modes)
+        bool adaptive;  // fused: refine only the ill-conditioned pixels
+        int mode() const
+        {
+            if (adaptive) return want_w ? FUSED_ADAPT_W : FUSED_ADAPT_ZP;
+            return scratch ? FUSED_REFINE : want_w ? FUSED_W : FUSED_ZP;
+        }
     };
     std::vector<Group> groups;
     for (int i = 0; i < n;) {
         const FrameDev &f = fs[i];
         if (use_fused(f, o)) {
-            Group g{0, i, 0, false, false, o.refine != 0};
+            Group g{0, i, 0, false, false, o.refine != 0, o.refine == COS_CAPON_REFINE_ADAPTIVE};
             int j = i;
             while (j < n && g.count < kMaxFrames && use_fused(fs[j], o) && fs[j].L == f.L && fs[j].K == f.K &&
                    fs[j].M == f.M) {
@@ -353,7 +358,7 @@ static int run_frames(cos_capon_ctx *c, const FrameDev *fs, int n, const cos_cap
             groups.push_back(g);
             i = j;
         } else {
-            groups.push_back(Group{f.Nb > 0 ? 1 : 2, i, 1, false, false, f.Nb == 0});
+            groups.push_back(Group{f.Nb > 0 ? 1 : 2, i, 1, false, false, f.Nb == 0, false});
             ++i;
         }
     }

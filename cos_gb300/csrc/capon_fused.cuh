@@ -355,12 +355,29 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
             const float4 *xw = xe + (size_t)lpc * XS;
 
             if constexpr (C::WIDE) {
+                constexpr bool ADAPT = MODE == FUSED_ADAPT_ZP || MODE == FUSED_ADAPT_W;
                 float4 *const stash =
-                    MODE == FUSED_REFINE
+                    (MODE == FUSED_REFINE || ADAPT)
                         ? fp.stash + ((size_t)blockIdx.x * C::WARPS * PPW + warp * PPW + gi) * WideStash<L, G>::Q
                         : nullptr;
-                wide_pixel<C, MODE>(f, xw, XS, Ns, cs + (size_t)lpc * L, cl + (size_t)lpc * L, gs + (size_t)lpc * L, rb,
-                                    stash, r, active, (size_t)bx * f.Npy + p, status);
+                const float2 *crow = cs + (size_t)lpc * L, *clrow = cl + (size_t)lpc * L, *grow = gs + (size_t)lpc * L;
+                const size_t pix = (size_t)bx * f.Npy + p;
+                if constexpr (ADAPT) {
+                    // every pixel in the z/P (w) mode; the ill-conditioned ones
+                    // again through the refinement pass, which overwrites their
+                    // outputs (decided per warp: both pixel groups of a warp at
+                    // G = 16 take the pass when either needs it)
+                    float spread = 0.f;
+                    wide_pixel<C, MODE == FUSED_ADAPT_W ? FUSED_W : FUSED_ZP>(f, xw, XS, Ns, crow, clrow, grow, rb,
+                                                                               nullptr, r, active, pix, status, &spread);
+                    if (__any_sync(0xffffffffu, spread > kAdaptiveSpread)) {
+                        __syncwarp();
+                        wide_pixel<C, FUSED_REFINE, true>(f, xw, XS, Ns, crow, clrow, grow, rb, stash, r, active, pix,
+                                                          status);
+                    }
+                } else {
+                    wide_pixel<C, MODE>(f, xw, XS, Ns, crow, clrow, grow, rb, stash, r, active, pix, status);
+                }
                 continue;
             }
             float2 A[L][NM];
@@ -755,11 +772,13 @@ size_t stash_bytes(int num_sms)
     if constexpr (!C::WIDE) {
         return 0;
     } else {
-        int per_sm = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fused_kernel<C, FUSED_REFINE>, C::WARPS * 32, 0) !=
-            cudaSuccess) {
-            cudaGetLastError();
-            return 0;
+        int per_sm = 0, q = 0;
+        for (auto k : {fused_kernel<C, FUSED_REFINE>, fused_kernel<C, FUSED_ADAPT_ZP>, fused_kernel<C, FUSED_ADAPT_W>}) {
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&q, k, C::WARPS * 32, 0) != cudaSuccess) {
+                cudaGetLastError();
+                return 0;
+            }
+            per_sm = q > per_sm ? q : per_sm;
         }
         return (size_t)num_sms * per_sm * C::WARPS * C::PPW * WideStash<C::L, C::G>::Q * sizeof(float4);
     }
@@ -791,25 +810,47 @@ int launch_cfg(FramesParam fp, unsigned *status, int num_sms, cudaStream_t s)
     if (per_sm < 1) return cudaErrorNotSupported;
     long long grid = (long long)num_sms * per_sm;
     if (grid > begin) grid = begin;
-    if (MODE == FUSED_REFINE &&
+    if ((MODE == FUSED_REFINE || MODE == FUSED_ADAPT_ZP || MODE == FUSED_ADAPT_W) &&
         (!fp.stash || fp.stash_bytes < (size_t)grid * C::WARPS * C::PPW * WideStash<C::L, C::G>::Q * sizeof(float4)))
         return cudaErrorNotSupported;
     fused_kernel<C, MODE><<<(unsigned)grid, C::WARPS * 32, S.total, s>>>(fp, begin, status);
     return cudaGetLastError();
 }
 
+// z/P, w and R modes
 template <class C>
-int launch_any(const FramesParam &fp, int mode, unsigned *status, int num_sms, cudaStream_t s)
+int launch_basic(const FramesParam &fp, int mode, unsigned *status, int num_sms, cudaStream_t s)
 {
     switch (mode) {
     case FUSED_ZP: return launch_cfg<C, FUSED_ZP>(fp, status, num_sms, s);
     case FUSED_W: return launch_cfg<C, FUSED_W>(fp, status, num_sms, s);
     case FUSED_R: return launch_cfg<C, FUSED_R>(fp, status, num_sms, s);
-    case FUSED_REFINE:
-        if constexpr (C::WIDE) return launch_cfg<C, FUSED_REFINE>(fp, status, num_sms, s);
-        return cudaErrorNotSupported;
-    default: return cudaErrorInvalidValue;
+    default: return cudaErrorNotSupported;
     }
+}
+
+// the refinement modes (L > 32; the wide instantiation files compile them in
+// a translation unit of their own, in parallel with the others)
+template <class C>
+int launch_refining(const FramesParam &fp, int mode, unsigned *status, int num_sms, cudaStream_t s)
+{
+    if constexpr (!C::WIDE) {
+        return cudaErrorNotSupported;
+    } else {
+        switch (mode) {
+        case FUSED_REFINE: return launch_cfg<C, FUSED_REFINE>(fp, status, num_sms, s);
+        case FUSED_ADAPT_ZP: return launch_cfg<C, FUSED_ADAPT_ZP>(fp, status, num_sms, s);
+        case FUSED_ADAPT_W: return launch_cfg<C, FUSED_ADAPT_W>(fp, status, num_sms, s);
+        default: return cudaErrorNotSupported;
+        }
+    }
+}
+
+template <class C>
+int launch_any(const FramesParam &fp, int mode, unsigned *status, int num_sms, cudaStream_t s)
+{
+    return mode <= FUSED_R ? launch_basic<C>(fp, mode, status, num_sms, s)
+                           : launch_refining<C>(fp, mode, status, num_sms, s);
 }
 
 }  // namespace fused

@@ -1,18 +1,23 @@
-// Fused element-space kernel instantiation for L = 48, temporal window T = 3:
-// two pixels per warp (16 lanes each, three columns per lane), the blocked
-// per-pixel path of capon_fused_wide.cuh; any channel count.
-#include "capon_fused.cuh"
+// Candidate table of the fused element-space kernel for L = 48, temporal window T = 3; the
+// configurations are compiled in the capon_fused_l48_t3?[_refine].cu files.
+// The autotuner in capon_api.cu picks one per (L, K, M, mode) shape; a
+// candidate compiled for a fixed M reports cudaErrorNotSupported for other M.
+#include "capon_internal.h"
 
 namespace cgb {
+int fused_l48_t3a_launch(const FramesParam &fp, int mode, unsigned *st, int n, cudaStream_t s);
+int fused_l48_t3a_launch_refine(const FramesParam &fp, int mode, unsigned *st, int n, cudaStream_t s);
+size_t fused_l48_t3a_smem(int K, int M);
+size_t fused_l48_t3a_stash(int num_sms);
+
 namespace {
-using C0 = fused::Cfg<48, 16, 8, 1, 3, 0, true>;
-int launch_0(const FramesParam &fp, int mode, unsigned *st, int n, cudaStream_t s)
+int launch_l48_t3a(const FramesParam &fp, int mode, unsigned *st, int n, cudaStream_t s)
 {
-    return fused::launch_any<C0>(fp, mode, st, n, s);
+    return mode <= FUSED_R ? fused_l48_t3a_launch(fp, mode, st, n, s) : fused_l48_t3a_launch_refine(fp, mode, st, n, s);
 }
 
 const FusedCandidate kCand[] = {
-    {"L48.G16.W8.N1.sync.T3", 48, 3, 0, launch_0, fused::smem_bytes<C0>, fused::stash_bytes<C0>},
+    {"L48.G16.W8.N1.sync.T3", 48, 3, 0, launch_l48_t3a, fused_l48_t3a_smem, fused_l48_t3a_stash},
 };
 }  // namespace
 

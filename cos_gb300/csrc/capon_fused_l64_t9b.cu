@@ -1,15 +1,14 @@
-// Fused element-space kernel for L = 64, temporal window T = 9, 8 warps, M = 128
-// (one warp per pixel, the blocked per-pixel path of capon_fused_wide.cuh).
-// One configuration per file so that the configurations compile in parallel;
-// the candidate table is in capon_fused_l64_t9.cu.
+// Fused element-space kernel, L = 64, T = 9, 8 warps, M = 128: the z/P, w and R modes (the
+// blocked per-pixel path of capon_fused_wide.cuh).  The refinement modes of
+// the same configuration are in capon_fused_l64_t9b_refine.cu, so that the two
+// compile in parallel; the candidate table is in capon_fused_l64_t9.cu.
 #include "capon_fused.cuh"
 
 namespace cgb {
-using CL64T9b = fused::Cfg<64, 32, 8, 2, 9, 128, false>;
+using CL64T9B = fused::Cfg<64, 32, 8, 2, 9, 128, false>;
 int fused_l64_t9b_launch(const FramesParam &fp, int mode, unsigned *st, int n, cudaStream_t s)
 {
-    return fused::launch_any<CL64T9b>(fp, mode, st, n, s);
+    return fused::launch_basic<CL64T9B>(fp, mode, st, n, s);
 }
-size_t fused_l64_t9b_smem(int K, int M) { return fused::smem_bytes<CL64T9b>(K, M); }
-size_t fused_l64_t9b_stash(int num_sms) { return fused::stash_bytes<CL64T9b>(num_sms); }
+size_t fused_l64_t9b_smem(int K, int M) { return fused::smem_bytes<CL64T9B>(K, M); }
 }  // namespace cgb

@@ -109,10 +109,15 @@ COS_DEV void ff_cmac(float2 &h, float2 &l, float4 a, float2 xa, float2 xb)
     l = ffma2(make_float2(a.w, a.w), xb, l);
 }
 
-template <class C, int MODE>
+// MODE: FUSED_ZP, FUSED_W, FUSED_R or FUSED_REFINE.  OWN_R0: the first
+// covariance row is formed here, with exact products, from the pixel's own
+// range rows (the refinement pass of the adaptive mode, whose tile carries
+// the ordinary rows).  spread (z/P and w modes): the factorisation's pivot
+// spread max d_i / min d_i, which the adaptive mode tests.
+template <class C, int MODE, bool OWN_R0 = false>
 COS_DEV void wide_pixel(const FrameDev &f, const float4 *xw, const int XS, const int Ns, const float2 *crow,
                         const float2 *clrow, const float2 *grow, float4 *area, float4 *stash, const int r,
-                        const bool active, const size_t pix, unsigned *status)
+                        const bool active, const size_t pix, unsigned *status, float *spread = nullptr)
 {
     constexpr int L = C::L, G = C::G, NM = C::NM, T = C::T;
     // the w and the refinement modes carry the right-hand side a only and keep
@@ -130,9 +135,28 @@ COS_DEV void wide_pixel(const FrameDev &f, const float4 *xw, const int XS, const
     for (int m = 0; m < NM; ++m) {
         const int j = m * G + r;
         float2 h = make_float2(0.f, 0.f), l = make_float2(0.f, 0.f);
-        for (int t = 0; t < T; ++t) {
-            two_sum_acc(h, l, crow[t * L + j]);
-            l = fadd2(l, clrow[t * L + j]);
+        if constexpr (OWN_R0) {
+            // sum_t sum_s x_t[s] conj(x_t[s+j]), exact products (TwoProd by fma)
+            for (int t = 0; t < T; ++t) {
+                const float4 *xr = xw + t * XS;
+#pragma unroll 4
+                for (int s = 0; s < Ns; ++s) {
+                    const float4 a = xr[s], c = xr[s + j];
+                    const float2 an = make_float2(a.x, a.y), az = make_float2(a.z, a.w);
+                    const float2 sr = make_float2(c.x, c.x), si = make_float2(c.y, c.y);
+                    const float2 p1 = fmul2(sr, an), p2 = fmul2(si, az);
+                    const float2 e = fadd2(ffma2(sr, an, make_float2(-p1.x, -p1.y)),
+                                           ffma2(si, az, make_float2(-p2.x, -p2.y)));
+                    two_sum_acc(h, l, p1);
+                    two_sum_acc(h, l, p2);
+                    l = fadd2(l, e);
+                }
+            }
+        } else {
+            for (int t = 0; t < T; ++t) {
+                two_sum_acc(h, l, crow[t * L + j]);
+                l = fadd2(l, clrow[t * L + j]);
+            }
         }
         const float2 s = fadd2(h, l);
         r0h[j] = s;
@@ -165,6 +189,7 @@ COS_DEV void wide_pixel(const FrameDev &f, const float4 *xw, const int XS, const
     float2 b1[NM], b2[NM];  // right-hand sides a = 1 and g, rows m*G + r
     float dinv[NM];         // w and refinement modes: 1/d of the lane's own rows
     bool bad = false;
+    float dmin = 3.0e38f, dmax = 0.f;  // pivot range
     float s11 = 0.f;
     float2 s12 = make_float2(0.f, 0.f);
 #pragma unroll
@@ -375,6 +400,8 @@ COS_DEV void wide_pixel(const FrameDev &f, const float4 *xw, const int XS, const
                 const float dv = -buf[i].x;
                 const float4 yy = buf[L];
                 bad |= !(dv > 0.f);
+                dmin = fminf(dmin, dv);
+                dmax = fmaxf(dmax, dv);
                 const float rdv = __frcp_rn(dv);
                 if (b + 1 < NM && r == 0) dinv_s[i] = rdv;
                 if (WMODE && r == oi) dinv[b] = rdv;
@@ -415,6 +442,7 @@ COS_DEV void wide_pixel(const FrameDev &f, const float4 *xw, const int XS, const
         }
     });
     if constexpr (MODE == FUSED_R) return;
+    if (spread) *spread = bad ? 3.0e38f : dmax / dmin;
 
     // ---- outputs (s11, and in the z/P mode s12, are complete on every lane)
     if (MODE != FUSED_REFINE && active && r == 0) {

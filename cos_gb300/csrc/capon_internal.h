@@ -95,7 +95,17 @@ enum FusedMode : int {
     FUSED_W = 1,   // z, P and w (back substitution)
     FUSED_R = 2,   // the loaded covariance R only (no factorisation)
     FUSED_REFINE = 3,  // z, P (and w) with one refinement step of R^-1 a (L > 32)
+    // adaptive refinement (L > 32): the z/P (or w) mode on every pixel, then
+    // the refinement pass on the pixels whose pivot spread exceeds kAdaptiveSpread
+    FUSED_ADAPT_ZP = 4,
+    FUSED_ADAPT_W = 5,
 };
+// Pivot spread max d_i / min d_i of the square-root-free Cholesky above which
+// the adaptive mode refines a pixel.  On the precision stress data (L=64,
+// K=4, two coherent scatterers at 40 dB, loading 1e-3) the pixels below it
+// come within 1.6e-6 of FP64 without refinement (single-precision LAPACK on
+// the oracle's R).
+static constexpr float kAdaptiveSpread = 32.f;
 struct FusedCandidate {
     const char *name;
     int L;

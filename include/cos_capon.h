@@ -73,12 +73,21 @@ extern "C" {
 #define COS_CAPON_R_NORMALISED 1  /* R row-major, loaded, normalised by 1/((M-L+1)(2Yavg+1))
                                      (getCaponC.pyx:240-242)                                     */
 
+#define COS_CAPON_REFINE_NONE     0  /* FP32 Cholesky                                              */
+#define COS_CAPON_REFINE_ALL      1  /* one step of iterative refinement of R^-1 a with an FP64
+                                        residual on every pixel                                   */
+/* Element space with a fused kernel for L > 32 (L=48 with K=1, L=64 with K=4):
+   every pixel in the FP32 fused form, then the refinement step (with the
+   accurate covariance) on the pixels whose square-root-free Cholesky has a
+   pivot spread max d_i / min d_i above 32, the ill-conditioned ones.
+   Elsewhere the same as COS_CAPON_REFINE_ALL.                                */
+#define COS_CAPON_REFINE_ADAPTIVE 2
+
 typedef struct cos_capon_opts {
     int form;       /* COS_CAPON_FORM_*                                       */
     int loading;    /* COS_CAPON_LOAD_*                                       */
     int r_layout;   /* COS_CAPON_R_*                                          */
-    int refine;     /* 1: one step of iterative refinement of R^-1 a with an
-                       FP64 residual; 0: plain FP32 Cholesky                  */
+    int refine;     /* COS_CAPON_REFINE_*                                     */
     int fb;         /* 1: forward-backward averaged covariance (R + J R^T J)/2
                        before loading and any beamspace transform
                        (getCaponAllC.pyx:346-347, getCaponPy_ref.py:103-104);

@@ -172,3 +172,25 @@ def test_refinement_l48_and_loaded_covariance():
     eR = (np.abs(o["R"] - ref["R"]).reshape(2, npy, -1).max(-1)
           / np.abs(ref["R"]).reshape(2, npy, -1).max(-1))
     assert eR.max() <= 4e-7
+
+
+def test_adaptive_refinement_refines_only_ill_conditioned_pixels():
+    """opts.refine = 2: a pixel's outputs are either the plain fused form's,
+    bit for bit (pivot spread <= 32), or the refine-all form's (the pixels
+    above it; within 1e-6, the refinement pass forming its first covariance
+    row from the pixel's own rows, not the tile's), and the refined ones are
+    few.  The result meets the refined bar on the stress slice."""
+    from cos_gb300 import _lib
+    x, c = config3_slice()
+    ref = oracle.capon(x, c["d"], c["L"], c["K"], want_w=False, nthreads=3)
+    o0 = run(x, c["L"], c["K"], c["d"])
+    o1 = run(x, c["L"], c["K"], c["d"], refine=_lib.REFINE_ALL)
+    o2 = run(x, c["L"], c["K"], c["d"], refine=_lib.REFINE_ADAPTIVE)
+    plain = (o2["P"] == o0["P"]) & (o2["z"] == o0["z"])
+    close = np.abs(o2["P"] - o1["P"]) <= 1e-6 * o1["P"]
+    assert np.all(plain | close)
+    frac = 1.0 - plain.mean()
+    msg = check(o2, ref, f"config3 fused L64 adaptive ({frac:.1%} refined)")
+    assert 0 < frac < 0.3, msg
+    eP = np.abs(o2["P"] - ref["P"]) / ref["P"]
+    assert eP.max() <= 5e-5, msg
