@@ -139,15 +139,16 @@ static int candidates(int L, int K, int form, const FusedCandidate **out)
     if (L == 32 && T == 1) return fused_candidates_l32_t1(out);
     if (L == 32 && T == 3) return fused_candidates_l32_t3(out);
     if (L == 32 && T == 5) return fused_candidates_l32_t5(out);
-    if (L == 48 && T == 3) return fused_candidates_l48_t3(out);
-    if (L == 64 && T == 9) return fused_candidates_l64_t9(out);
+    if (L == 48) return fused_candidates_l48(out);
+    if (L == 64) return fused_candidates_l64(out);
     return 0;
 }
 
-// a candidate serves a frame when its compile-time L, T (and M) match
+// a candidate serves a frame when its compile-time L, T (0: any) and M (0: any) match
 static bool cand_fits(const FusedCandidate &c, const FrameDev &f)
 {
-    return c.L == f.L && c.T == 2 * f.K + 1 && (c.M == 0 || c.M == f.M) && c.smem(f.K, f.M) <= kFusedSmemMax;
+    return c.L == f.L && (c.T == 0 || c.T == 2 * f.K + 1) && (c.M == 0 || c.M == f.M) &&
+           c.smem(f.K, f.M) <= kFusedSmemMax;
 }
 
 // the fused kernels for L > 32 carry the refinement step themselves; for

@@ -101,14 +101,18 @@ COS_DEV void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.clust
 // ---- compile-time configuration --------------------------------------------
 // L: subarray length; G: lanes per pixel (lane r owns columns j = m*G + r);
 // WARPS x NITER x (32/G) pixels per tile; T: the temporal window 2K+1 (exact,
-// so the window loops carry no runtime bound); M: channel count, 0 = taken at
+// so the window loops carry no runtime bound; 0 = taken from the frame, for
+// the L > 32 path only, whose window loops are rolled); M: channel count, 0 = taken at
 // run time (a compile-time M turns every shared-memory offset of the unrolled
 // code into an immediate); SYNC: barrier points that keep the CTA's warps in
 // step, so that the long unrolled instruction stream is fetched once for all
 // of them.
 template <int L_, int G_, int WARPS_, int NITER_, int T_, int M_, bool SYNC_>
 struct Cfg {
-    static constexpr int L = L_, G = G_, WARPS = WARPS_, NITER = NITER_, T = T_, M = M_;
+    static constexpr int L = L_, G = G_, WARPS = WARPS_, NITER = NITER_, M = M_;
+    // RT_T: T from the frame; T then sizes only the unused L <= 32 code
+    static constexpr bool RT_T = T_ == 0;
+    static constexpr int T = RT_T ? 1 : T_;
     static constexpr bool SYNC = SYNC_;
     static constexpr int NM = L / G;       // column slots per lane
     static constexpr int PPW = 32 / G;     // pixels per warp
@@ -121,6 +125,7 @@ struct Cfg {
     static constexpr int AREA = WIDE ? WideArea<L, G>::Q : 2 * (L + 1);
     static constexpr int RBQ = AREA > (G * (G + 1) + 1) / 2 ? AREA : (G * (G + 1) + 1) / 2;
     static_assert(L % G == 0 && 32 % G == 0, "G must divide L and 32");
+    static_assert(WIDE || !RT_T, "a run-time window needs the L > 32 path");
 };
 
 // shared-memory carve-up (bytes), host and device agree
@@ -157,7 +162,7 @@ template <class C, int MODE>
 __global__ void __launch_bounds__(C::WARPS * 32, 1)
 fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsigned *status)
 {
-    constexpr int L = C::L, G = C::G, NM = C::NM, PPW = C::PPW, TILE = C::TILE, T = C::T, K = (C::T - 1) / 2;
+    constexpr int L = C::L, G = C::G, NM = C::NM, PPW = C::PPW, TILE = C::TILE, T = C::T;
     extern __shared__ __align__(128) unsigned char smem[];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int gi = lane / G, r = lane % G;
@@ -166,6 +171,7 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
     // all frames of one launch share K and M bounds through the first frame's
     // carve-up; the host groups frames so that K and M are equal within a launch
     const FrameDev &f0 = fp.f[0];
+    const int K = C::RT_T ? f0.K : (C::T - 1) / 2;
     const Smem S(TILE, K, C::M ? C::M : f0.M, L, C::WARPS, PPW, C::RBQ);
     float2 *raw[2] = {(float2 *)(smem + S.off_raw0), (float2 *)(smem + S.off_raw1)};
     float4 *xe = (float4 *)(smem + S.off_xe);
@@ -788,7 +794,7 @@ template <class C, int MODE>
 int launch_cfg(FramesParam fp, unsigned *status, int num_sms, cudaStream_t s)
 {
     const FrameDev &f0 = fp.f[0];
-    if (2 * f0.K + 1 != C::T) return cudaErrorNotSupported;
+    if (!C::RT_T && 2 * f0.K + 1 != C::T) return cudaErrorNotSupported;
     for (int i = 0; i < fp.n; ++i)
         if (C::M && fp.f[i].M != C::M) return cudaErrorNotSupported;
     long long begin = 0;

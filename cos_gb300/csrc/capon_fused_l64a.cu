@@ -1,0 +1,14 @@
+// Fused element-space kernel, L = 64, any T, 12 warps, M = 128: the z/P, w and R modes (the
+// blocked per-pixel path of capon_fused_wide.cuh).  The refinement modes of
+// the same configuration are in capon_fused_l64a_refine.cu, so that the two
+// compile in parallel; the candidate table is in capon_fused_l64.cu.
+#include "capon_fused.cuh"
+
+namespace cgb {
+using CL64A = fused::Cfg<64, 32, 12, 1, 0, 128, false>;
+int fused_l64a_launch(const FramesParam &fp, int mode, unsigned *st, int n, cudaStream_t s)
+{
+    return fused::launch_basic<CL64A>(fp, mode, st, n, s);
+}
+size_t fused_l64a_smem(int K, int M) { return fused::smem_bytes<CL64A>(K, M); }
+}  // namespace cgb

@@ -119,7 +119,8 @@ COS_DEV void wide_pixel(const FrameDev &f, const float4 *xw, const int XS, const
                         const float2 *clrow, const float2 *grow, float4 *area, float4 *stash, const int r,
                         const bool active, const size_t pix, unsigned *status, float *spread = nullptr)
 {
-    constexpr int L = C::L, G = C::G, NM = C::NM, T = C::T;
+    constexpr int L = C::L, G = C::G, NM = C::NM;
+    const int T = C::RT_T ? 2 * f.K + 1 : C::T;
     // the w and the refinement modes carry the right-hand side a only and keep
     // the factor for the back substitution
     constexpr bool WMODE = MODE == FUSED_W || MODE == FUSED_REFINE;

@@ -109,7 +109,7 @@ static constexpr float kAdaptiveSpread = 32.f;
 struct FusedCandidate {
     const char *name;
     int L;
-    int T;  // the temporal window 2K+1 the instantiation is compiled for
+    int T;  // the temporal window 2K+1 the instantiation is compiled for, 0 = any
     int M;  // the channel count it is compiled for, 0 = any
     int (*launch)(const FramesParam &fp, int mode, unsigned *status, int num_sms, cudaStream_t s);
     size_t (*smem)(int K, int M);  // dynamic shared memory of a launch for (K, M)
@@ -125,8 +125,8 @@ int fused_candidates_l16_t5(const FusedCandidate **out);
 int fused_candidates_l32_t1(const FusedCandidate **out);
 int fused_candidates_l32_t3(const FusedCandidate **out);
 int fused_candidates_l32_t5(const FusedCandidate **out);
-int fused_candidates_l48_t3(const FusedCandidate **out);
-int fused_candidates_l64_t9(const FusedCandidate **out);
+int fused_candidates_l48(const FusedCandidate **out);
+int fused_candidates_l64(const FusedCandidate **out);
 // tensor-core fused kernel (capon_tcf.cu): z and P only, compile-time (L, T, M)
 int tc_fused_candidates(const FusedCandidate **out);
 // adjoint of the output power

@@ -194,3 +194,19 @@ def test_adaptive_refinement_refines_only_ill_conditioned_pixels():
     assert 0 < frac < 0.3, msg
     eP = np.abs(o2["P"] - ref["P"]) / ref["P"]
     assert eP.max() <= 5e-5, msg
+
+
+@pytest.mark.parametrize("L,K,M", [(64, 1, 128), (64, 2, 96), (64, 0, 80), (48, 2, 96), (48, 4, 64), (48, 0, 80)])
+def test_other_temporal_windows(L, K, M):
+    """The L > 32 instantiations take the window 2K+1 from the frame: any K
+    whose tile fits in shared memory runs the fused kernel (z/P, w, and the
+    adaptive refinement)."""
+    from cos_gb300 import _lib, synth
+    x = synth.cube(70, 3, M, [10.0, 4.0], seed=L + K + M)
+    ref = oracle.capon(x, 0.01, L, K, nthreads=3)
+    check(run(x, L, K, 0.01), ref, f"L{L} K{K} M{M} z/P")
+    o = run(x, L, K, 0.01, want_w=True)
+    msg = check(o, ref, f"L{L} K{K} M{M} w mode")
+    ew = np.linalg.norm(o["w"] - ref["w"], axis=-1) / np.linalg.norm(ref["w"], axis=-1)
+    assert ew.max() <= 2e-3, msg
+    check(run(x, L, K, 0.01, refine=_lib.REFINE_ADAPTIVE), ref, f"L{L} K{K} M{M} adaptive")
