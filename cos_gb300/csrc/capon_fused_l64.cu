@@ -19,7 +19,16 @@ int fused_l64c_launch_refine(const FramesParam &fp, int mode, unsigned *st, int 
 size_t fused_l64c_smem(int K, int M);
 size_t fused_l64c_stash(int num_sms);
 
+int fused_l64d_launch(const FramesParam &fp, int mode, unsigned *st, int n, cudaStream_t s);
+int fused_l64d_launch_refine(const FramesParam &fp, int mode, unsigned *st, int n, cudaStream_t s);
+size_t fused_l64d_smem(int K, int M);
+size_t fused_l64d_stash(int num_sms);
+
 namespace {
+int launch_l64d(const FramesParam &fp, int mode, unsigned *st, int n, cudaStream_t s)
+{
+    return mode <= FUSED_R ? fused_l64d_launch(fp, mode, st, n, s) : fused_l64d_launch_refine(fp, mode, st, n, s);
+}
 int launch_l64a(const FramesParam &fp, int mode, unsigned *st, int n, cudaStream_t s)
 {
     return mode <= FUSED_R ? fused_l64a_launch(fp, mode, st, n, s) : fused_l64a_launch_refine(fp, mode, st, n, s);
@@ -36,7 +45,8 @@ int launch_l64c(const FramesParam &fp, int mode, unsigned *st, int n, cudaStream
 const FusedCandidate kCand[] = {
     {"L64.G32.W12.N1.M128", 64, 0, 128, launch_l64a, fused_l64a_smem, fused_l64a_stash},
     {"L64.G32.W8.N2.M128", 64, 0, 128, launch_l64b, fused_l64b_smem, fused_l64b_stash},
-    {"L64.G32.W8.N2", 64, 0, 0, launch_l64c, fused_l64c_smem, fused_l64c_stash},
+    {"L64.G32.W12.N1", 64, 0, 0, launch_l64c, fused_l64c_smem, fused_l64c_stash},
+    {"L64.G32.W8.N2", 64, 0, 0, launch_l64d, fused_l64d_smem, fused_l64d_stash},
 };
 }  // namespace
 

@@ -1,11 +1,11 @@
-// Fused element-space kernel, L = 64, any T, 8 warps, any M: the z/P, w and R modes (the
+// Fused element-space kernel, L = 64, any T, 12 warps, any M: the z/P, w and R modes (the
 // blocked per-pixel path of capon_fused_wide.cuh).  The refinement modes of
 // the same configuration are in capon_fused_l64c_refine.cu, so that the two
 // compile in parallel; the candidate table is in capon_fused_l64.cu.
 #include "capon_fused.cuh"
 
 namespace cgb {
-using CL64C = fused::Cfg<64, 32, 8, 2, 0, 0, false>;
+using CL64C = fused::Cfg<64, 32, 12, 1, 0, 0, false>;
 int fused_l64c_launch(const FramesParam &fp, int mode, unsigned *st, int n, cudaStream_t s)
 {
     return fused::launch_basic<CL64C>(fp, mode, st, n, s);

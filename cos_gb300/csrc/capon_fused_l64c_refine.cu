@@ -1,9 +1,9 @@
-// Fused element-space kernel, L = 64, any T, 8 warps, any M: the refinement modes
+// Fused element-space kernel, L = 64, any T, 12 warps, any M: the refinement modes
 // (every pixel, or the ill-conditioned ones), with the bytes of stash they need.
 #include "capon_fused.cuh"
 
 namespace cgb {
-using CL64C = fused::Cfg<64, 32, 8, 2, 0, 0, false>;
+using CL64C = fused::Cfg<64, 32, 12, 1, 0, 0, false>;
 int fused_l64c_launch_refine(const FramesParam &fp, int mode, unsigned *st, int n, cudaStream_t s)
 {
     return fused::launch_refining<CL64C>(fp, mode, st, n, s);
