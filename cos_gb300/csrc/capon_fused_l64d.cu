@@ -1,5 +1,6 @@
-// Fused element-space kernel, L = 64, any T, 8 warps, any M (its smaller tile fits larger M): the z/P, w and R modes (the
-// blocked per-pixel path of capon_fused_wide.cuh).  The refinement modes of
+// Fused element-space kernel, L = 64, any T, 8 warps, any M (its smaller tile
+// fits larger M than the 12-warp one): the z/P, w and R modes (the blocked
+// per-pixel path of capon_fused_wide.cuh).  The refinement modes of
 // the same configuration are in capon_fused_l64d_refine.cu, so that the two
 // compile in parallel; the candidate table is in capon_fused_l64.cu.
 #include "capon_fused.cuh"
