@@ -76,7 +76,7 @@ extern "C" {
 #define COS_CAPON_REFINE_NONE     0  /* FP32 Cholesky                                              */
 #define COS_CAPON_REFINE_ALL      1  /* one step of iterative refinement of R^-1 a with an FP64
                                         residual on every pixel                                   */
-/* Element space with a fused kernel for L > 32 (L=48 with K=1, L=64 with K=4):
+/* Element space with a fused kernel for L > 32 (L = 48 and 64, any K whose tile fits):
    every pixel in the FP32 fused form, then the refinement step (with the
    accurate covariance) on the pixels whose square-root-free Cholesky has a
    pivot spread max d_i / min d_i above 32, the ill-conditioned ones.
