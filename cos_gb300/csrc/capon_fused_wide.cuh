@@ -20,17 +20,30 @@
 // This is the right-looking order with each block's updates deferred until
 // its rows exist: the same arithmetic, but at most (b+1) G (L/G - b) column
 // slots are live at a time (64 of the 96 a lane's columns span at L = 64), so
-// the factor stays in the 255 registers of a thread.
+// the factor stays in registers (255 a thread at 8 warps, 168 at 12, with a
+// few spills).
 //
 // Why float-float S: with Ns = M - L + 1 subarrays no longer many times L,
 // S[k, .] is not small next to R (at L = 64, M = 128 row 63 spans 63 of the
 // 65 subarray rows), and an FP32 running sum would round values as large as
-// R 63 times.  Each increment D (2T products of a few hundredths of R at
-// most) is summed in FP32, t outer, straight into the slot that later holds R.
+// R 63 times.  In the z/P, w and R modes each increment D (2T products of a
+// few hundredths of R at most) is summed in FP32, t outer, straight into the
+// slot that later holds R.  The refinement mode adds each range row's
+// increment to S by TwoSum instead, and forms the first row with exact
+// products: its residual is only as good as this matrix.
+//
+// Refinement (FUSED_REFINE): the float-float R goes to a per-warp stash, and
+// after the factorisation x0 = R~^-1 a is corrected once by the FP64-assembled
+// residual a - (R + dl I) x0.  The adaptive modes (FUSED_ADAPT_*) run the z/P
+// or w mode on every pixel and the refinement pass on the pixels whose pivot
+// spread exceeds kAdaptiveSpread.
 //
 // The trace for the loading is needed before block 0 is factored, when most
 // rows do not exist yet; it is summed directly,
 //   tr(R) = L R0[0] + sum_{k=1}^{L-1} (L - k) D[k,k].
+//
+// The temporal window T = 2K+1 may be a run-time value (Cfg T = 0): every
+// window loop of this path is rolled.
 #pragma once
 #include <type_traits>
 
