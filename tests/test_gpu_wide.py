@@ -210,3 +210,38 @@ def test_other_temporal_windows(L, K, M):
     ew = np.linalg.norm(o["w"] - ref["w"], axis=-1) / np.linalg.norm(ref["w"], axis=-1)
     assert ew.max() <= 2e-3, msg
     check(run(x, L, K, 0.01, refine=_lib.REFINE_ADAPTIVE), ref, f"L{L} K{K} M{M} adaptive")
+
+
+@pytest.mark.parametrize("refine", [0, 2])
+def test_graph_replay_equals_eager_call(refine):
+    """A frame of the L > 32 kernels (z/P, and the adaptive refinement whose
+    pass uses the context's stash) captured into a CUDA graph after a warm
+    call: each replay writes the eager call's outputs bit for bit."""
+    import torch
+    from cos_gb300 import _lib, capon
+    x, c = config3_slice(Nx=2, Ny=120)
+    xt = torch.from_numpy(x).cuda()
+    ctx = capon.Context()
+    o = capon.opts(form=_lib.FORM_FUSED, refine=refine)
+
+    def frame():
+        f = capon.DeviceFrame(x=xt, L=c["L"], K=c["K"], d=c["d"])
+        f.P = torch.empty((2, 120 - 2 * c["K"]), dtype=torch.float32, device="cuda")
+        return f
+
+    s = torch.cuda.Stream()
+    eager = frame()
+    with torch.cuda.stream(s):
+        for _ in range(2):   # tunes the shape and sizes the stash
+            capon.capon_frames([eager], ctx, o, stream=s)
+    s.synchronize()
+    gf = frame()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        capon.capon_frames([gf], ctx, o, stream=s)
+    for _ in range(2):
+        gf.P.zero_()
+        g.replay()
+        torch.cuda.synchronize()
+        assert np.array_equal(gf.P.cpu().numpy(), eager.P.cpu().numpy())
+        assert np.array_equal(gf.z.cpu().numpy(), eager.z.cpu().numpy())
