@@ -196,11 +196,13 @@ def test_adaptive_refinement_refines_only_ill_conditioned_pixels():
     assert eP.max() <= 5e-5, msg
 
 
-@pytest.mark.parametrize("L,K,M", [(64, 1, 128), (64, 2, 96), (64, 0, 80), (48, 2, 96), (48, 4, 64), (48, 0, 80)])
+@pytest.mark.parametrize("L,K,M", [(64, 1, 128), (64, 2, 96), (64, 0, 80), (64, 2, 101), (48, 2, 96), (48, 4, 64),
+                                   (48, 0, 80)])
 def test_other_temporal_windows(L, K, M):
     """The L > 32 instantiations take the window 2K+1 from the frame: any K
     whose tile fits in shared memory runs the fused kernel (z/P, w, and the
-    adaptive refinement)."""
+    adaptive refinement).  M = 101: range rows not 16-byte aligned, staged
+    with plain loads instead of the bulk copy."""
     from cos_gb300 import _lib, synth
     x = synth.cube(70, 3, M, [10.0, 4.0], seed=L + K + M)
     ref = oracle.capon(x, 0.01, L, K, nthreads=3)
