@@ -144,18 +144,22 @@ static int candidates(int L, int K, int form, const FusedCandidate **out)
     return 0;
 }
 
-// a candidate serves a frame when its compile-time L, T (0: any) and M (0: any) match
-static bool cand_fits(const FusedCandidate &c, const FrameDev &f)
+// a candidate serves a frame when its compile-time L, T (0: any) and M (0: any)
+// match and it has the mode: the refinement modes where it carries a stash,
+// the others where it is not a refinement-only instantiation
+static bool cand_fits(const FusedCandidate &c, const FrameDev &f, bool refining)
 {
+    if (refining ? !c.stash : c.refine_only) return false;
     return c.L == f.L && (c.T == 0 || c.T == 2 * f.K + 1) && (c.M == 0 || c.M == f.M) &&
            c.smem(f.K, f.M) <= kFusedSmemMax;
 }
+static bool refining_mode(int mode) { return mode > FUSED_R; }
 
-// the fused kernels for L > 32 carry the refinement step themselves; for
-// L <= 32 it runs in the precise pipeline
+// the fused path carries the refinement step itself at L = 32 and above (the
+// blocked per-pixel path); at L = 16 it runs in the precise pipeline
 static bool refine_in_fused(const FrameDev &f, const cos_capon_opts &o)
 {
-    return o.form == COS_CAPON_FORM_FUSED && f.L > 32;
+    return o.form == COS_CAPON_FORM_FUSED && f.L >= 32;
 }
 
 static bool use_fused(const FrameDev &f, const cos_capon_opts &o)
@@ -165,7 +169,7 @@ static bool use_fused(const FrameDev &f, const cos_capon_opts &o)
     const FusedCandidate *c = nullptr;
     const int n = candidates(f.L, f.K, o.form, &c);
     for (int i = 0; i < n; ++i)
-        if (cand_fits(c[i], f)) return true;
+        if (cand_fits(c[i], f, o.refine != 0)) return true;
     return false;
 }
 
@@ -183,7 +187,7 @@ static int launch_fused_tuned(cos_capon_ctx *c, const FramesParam &fp, int mode,
     std::vector<int> ok;
     for (int i = 0; i < n; ++i) {
         bool fits = true;
-        for (int q = 0; q < fp.n; ++q) fits &= cand_fits(cand[i], fp.f[q]);
+        for (int q = 0; q < fp.n; ++q) fits &= cand_fits(cand[i], fp.f[q], refining_mode(mode));
         if (fits) ok.push_back(i);
     }
     if (ok.empty()) return COS_CAPON_ERR_NOT_SUPPORTED;
@@ -382,7 +386,7 @@ static int run_frames(cos_capon_ctx *c, const FrameDev *fs, int n, const cos_cap
                 const int nc = candidates(f.L, f.K, o.form, &cand);
                 size_t need = 0;
                 for (int q = 0; q < nc; ++q)
-                    if (cand[q].stash && cand_fits(cand[q], f)) need = std::max(need, cand[q].stash(c->num_sms));
+                    if (cand_fits(cand[q], f, true)) need = std::max(need, cand[q].stash(c->num_sms));
                 if (need == 0) return COS_CAPON_ERR_NOT_SUPPORTED;
                 if (int e = c->stash.ensure(need)) return e;
                 fp.stash = (float4 *)c->stash.p;

@@ -107,7 +107,7 @@ COS_DEV void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.clust
 // code into an immediate); SYNC: barrier points that keep the CTA's warps in
 // step, so that the long unrolled instruction stream is fetched once for all
 // of them.
-template <int L_, int G_, int WARPS_, int NITER_, int T_, int M_, bool SYNC_>
+template <int L_, int G_, int WARPS_, int NITER_, int T_, int M_, bool SYNC_, bool WIDE_ = (L_ > 32)>
 struct Cfg {
     static constexpr int L = L_, G = G_, WARPS = WARPS_, NITER = NITER_, M = M_;
     // RT_T: T from the frame; T then sizes only the unused L <= 32 code
@@ -117,8 +117,9 @@ struct Cfg {
     static constexpr int NM = L / G;       // column slots per lane
     static constexpr int PPW = 32 / G;     // pixels per warp
     static constexpr int TILE = WARPS * PPW * NITER;
-    // L > 32: the blocked per-pixel path of capon_fused_wide.cuh
-    static constexpr bool WIDE = L > 32;
+    // the blocked per-pixel path of capon_fused_wide.cuh: always for L > 32;
+    // at L <= 32 an instantiation of it serves the refinement modes
+    static constexpr bool WIDE = WIDE_;
     // float4 slots of a pixel group's shared area: the pivot-row buffers (and,
     // wide, the first covariance row and the 1/d of factored rows), or the
     // G x (G+1) exchange area of the w mode's back substitution
@@ -850,6 +851,14 @@ int launch_refining(const FramesParam &fp, int mode, unsigned *status, int num_s
         default: return cudaErrorNotSupported;
         }
     }
+}
+
+// the refinement modes alone (an L <= 32 instantiation of the blocked path,
+// which serves refinement next to the L <= 32 kernel's own modes)
+template <class C>
+int launch_refine_only(const FramesParam &fp, int mode, unsigned *status, int num_sms, cudaStream_t s)
+{
+    return mode <= FUSED_R ? (int)cudaErrorNotSupported : launch_refining<C>(fp, mode, status, num_sms, s);
 }
 
 template <class C>

@@ -113,8 +113,12 @@ struct FusedCandidate {
     int M;  // the channel count it is compiled for, 0 = any
     int (*launch)(const FramesParam &fp, int mode, unsigned *status, int num_sms, cudaStream_t s);
     size_t (*smem)(int K, int M);  // dynamic shared memory of a launch for (K, M)
-    // FUSED_REFINE: bytes of FramesParam::stash a launch needs (0: no refinement mode)
+    // the refinement modes: bytes of FramesParam::stash a launch needs (null:
+    // the candidate has no refinement modes)
     size_t (*stash)(int num_sms);
+    // serves the refinement modes only (the L <= 32 instantiation of the
+    // blocked path); the others serve the z/P, w and R modes
+    bool refine_only;
 };
 // shared memory one CTA may use; a candidate whose tile needs more for a
 // frame's (K, M) is not used for it (the precise pipeline takes the frame)

@@ -247,3 +247,26 @@ def test_graph_replay_equals_eager_call(refine):
         torch.cuda.synchronize()
         assert np.array_equal(gf.P.cpu().numpy(), eager.P.cpu().numpy())
         assert np.array_equal(gf.z.cpu().numpy(), eager.z.cpu().numpy())
+
+
+def test_refinement_at_l32():
+    """L = 32 (config-1 shape): refinement on every pixel and the adaptive
+    mode run in the fused path, through the one-warp-per-pixel instantiation
+    of the blocked path; z/P without refinement stays with the L = 32
+    kernel."""
+    from cos_gb300 import _lib, synth
+    c = synth.config1(seed=1, Nx=4, Ny=300)
+    x = c["x"]
+    ref = oracle.capon(x, c["d"], c["L"], c["K"], nthreads=4)
+    o1 = run(x, c["L"], c["K"], c["d"], want_w=True, refine=_lib.REFINE_ALL)
+    msg = check(o1, ref, "L32 refined")
+    eP = np.abs(o1["P"] - ref["P"]) / ref["P"]
+    ew = np.linalg.norm(o1["w"] - ref["w"], axis=-1) / np.linalg.norm(ref["w"], axis=-1)
+    assert eP.max() <= 1e-6 and ew.max() <= 1e-5, msg
+    o0 = run(x, c["L"], c["K"], c["d"])
+    o2 = run(x, c["L"], c["K"], c["d"], refine=_lib.REFINE_ADAPTIVE)
+    check(o2, ref, "L32 adaptive")
+    # config-1 data is well conditioned: the adaptive mode's first pass (the
+    # blocked path's z/P, not the L = 32 kernel's) decides for most pixels
+    plain = o2["P"] != o1["P"]
+    assert plain.mean() > 0.5
