@@ -288,9 +288,9 @@ def run_gpu(args) -> None:
                               P=torch.empty((NX, npy), dtype=torch.float32, device="cuda"))
         return f
 
-    def time_form(form: int, steps: int, warmup: int, clk=None):
+    def time_form(form: int, steps: int, warmup: int, clk=None, refine: int = 0):
         f = frame()
-        o = capon.opts(form=form)
+        o = capon.opts(form=form, refine=refine)
         with torch.cuda.stream(stream):
             for _ in range(warmup):
                 capon.capon_frames([f], ctx, o, stream)
@@ -330,6 +330,18 @@ def run_gpu(args) -> None:
     except Exception as exc:
         f_tcf = None
         tcf = {"error": str(exc)[:200]}
+
+    # the FP32 Cholesky with one FP64-residual refinement step, in the fused
+    # path: on every pixel, and on the ill-conditioned ones (pivot spread > 32)
+    refined, f_ref = {}, {}
+    for name, rv in (("all_pixels", _lib.REFINE_ALL), ("adaptive", _lib.REFINE_ADAPTIVE)):
+        try:
+            ms_r, f_ref[name] = time_form(_lib.FORM_FUSED, max(2, min(args.steps, 5)), max(1, min(args.warmup, 2)),
+                                          refine=rv)
+            refined[name] = {"ms_per_step": ms_r, "value": replicas.aggregate_rate(NPIX, ms_r, world),
+                             "unit": "pixels/s"}
+        except Exception as exc:
+            refined[name] = {"error": str(exc)[:200]}
 
     # e2e through the host-pointer C-ABI call, pinned host buffers
     xp = torch.from_numpy(x_host).pin_memory()
@@ -460,6 +472,9 @@ def run_gpu(args) -> None:
     if f_tcf is not None:
         eT = np.abs(f_tcf.P.cpu().numpy()[beams] - refo["P"]) / refo["P"]
         tcf["P_rel_err_max"], tcf["P_rel_err_median"] = float(eT.max()), float(np.median(eT))
+    for name, fr in f_ref.items():
+        eR = np.abs(fr.P.cpu().numpy()[beams] - refo["P"]) / refo["P"]
+        refined[name]["P_rel_err_max"], refined[name]["P_rel_err_median"] = float(eR.max()), float(np.median(eR))
 
     peaks = _peaks()
     fp32 = fp32_peak_tflops(torch)
@@ -474,6 +489,7 @@ def run_gpu(args) -> None:
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator, 8 scatterers, 20 dB)",
         "config": CONFIG,
         "tc_fused": tcf,
+        "refined": refined,
         "plain": {"value": NPIX * world / (ms_plain * 1e-3), "ms_per_step": ms_plain,
                   "speedup_fused_over_plain": ms_plain / ms},
         "parity": {"P_rel_err_max": float(relP.max()), "P_rel_err_median": float(np.median(relP)),
