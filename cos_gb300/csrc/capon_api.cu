@@ -155,11 +155,12 @@ static bool cand_fits(const FusedCandidate &c, const FrameDev &f, bool refining)
 }
 static bool refining_mode(int mode) { return mode > FUSED_R; }
 
-// the fused path carries the refinement step itself at L = 32 and above (the
-// blocked per-pixel path); at L = 16 it runs in the precise pipeline
-static bool refine_in_fused(const FrameDev &f, const cos_capon_opts &o)
+// the fused path carries the refinement step itself (the blocked per-pixel
+// path, instantiated for the refinement modes next to the L = 16 and 32
+// kernels); shapes without a fused kernel refine in the precise pipeline
+static bool refine_in_fused(const FrameDev &, const cos_capon_opts &o)
 {
-    return o.form == COS_CAPON_FORM_FUSED && f.L >= 32;
+    return o.form == COS_CAPON_FORM_FUSED;
 }
 
 static bool use_fused(const FrameDev &f, const cos_capon_opts &o)

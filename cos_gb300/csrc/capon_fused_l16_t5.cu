@@ -4,6 +4,10 @@
 #include "capon_fused.cuh"
 
 namespace cgb {
+int fused_l16r_launch(const FramesParam &fp, int mode, unsigned *st, int n, cudaStream_t s);
+size_t fused_l16r_smem(int K, int M);
+size_t fused_l16r_stash(int num_sms);
+
 namespace {
 int launch_0(const FramesParam &fp, int mode, unsigned *st, int n, cudaStream_t s)
 {
@@ -22,6 +26,8 @@ const FusedCandidate kCand[] = {
     {"L16.G4.W8.N1.sync.M32.T5", 16, 5, 32, launch_0, fused::smem_bytes<fused::Cfg<16, 4, 8, 1, 5, 32, true>>},
     {"L16.G4.W8.N1.M32.T5", 16, 5, 32, launch_1, fused::smem_bytes<fused::Cfg<16, 4, 8, 1, 5, 32, false>>},
     {"L16.G4.W8.N1.sync.T5", 16, 5, 0, launch_2, fused::smem_bytes<fused::Cfg<16, 4, 8, 1, 5, 0, true>>},
+    // the refinement modes (capon_fused_l16r.cu)
+    {"L16.G16.W8.refine", 16, 0, 0, fused_l16r_launch, fused_l16r_smem, fused_l16r_stash, true},
 };
 }  // namespace
 

@@ -76,13 +76,13 @@ extern "C" {
 #define COS_CAPON_REFINE_NONE     0  /* FP32 Cholesky                                              */
 #define COS_CAPON_REFINE_ALL      1  /* one step of iterative refinement of R^-1 a with an FP64
                                         residual on every pixel                                   */
-/* Element space on the fused path at L = 32, 48 and 64: every pixel in the
-   FP32 fused form of the one-warp-per-pixel kernels, then the refinement step
-   (with the accurate covariance) on the pixels whose square-root-free
-   Cholesky has a pivot spread max d_i / min d_i above 32, the ill-conditioned
-   ones.  Elsewhere the same as COS_CAPON_REFINE_ALL.  (Both refinement
-   values run in the fused kernels at L >= 32; at L = 16, and with any other
-   form, in the precise pipeline.)                                            */
+/* Element space on the fused path (L = 16, 32, 48, 64): every pixel in the
+   FP32 form of the blocked per-pixel kernels, then the refinement step (with
+   the accurate covariance) on the pixels whose square-root-free Cholesky has
+   a pivot spread max d_i / min d_i above 32, the ill-conditioned ones.
+   Elsewhere the same as COS_CAPON_REFINE_ALL.  (Both refinement values run
+   inside the fused kernels for the shapes they serve; other shapes and forms
+   refine in the precise pipeline.)                                           */
 #define COS_CAPON_REFINE_ADAPTIVE 2
 
 typedef struct cos_capon_opts {

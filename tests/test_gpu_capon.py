@@ -484,3 +484,23 @@ def test_side_by_side_frames_equal_serial_launches():
     for (za, pa), (zb, pb), (zc, pc) in zip(grab(ser), grab(par), grab(gr)):
         assert np.array_equal(za, zb) and np.array_equal(pa, pb)
         assert np.array_equal(za, zc) and np.array_equal(pa, pc)
+
+
+def test_precise_pipeline_refinement_with_exact_covariance(cap):
+    """The precise pipeline (R materialised in float-float with every product
+    exact, FP32 Cholesky, one FP64-residual step), which the plain form with
+    refine=1 and the shapes without a fused kernel take: on the L=64 stress
+    data it reaches 1e-6, the accuracy the fused refinement's FP32 increments
+    stop short of."""
+    from cos_gb300 import _lib, synth
+    x = synth.cube(96, 3, 128, [100.0, 100.0], seed=3, coherent_pair=True)
+    ref = oracle.capon(x, 1e-3, 64, 4, nthreads=3)
+    Npy = x.shape[1] - 8
+    z = np.zeros((3, Npy), np.complex64)
+    P = np.zeros((3, Npy), np.float32)
+    w = np.zeros((3, Npy, 64), np.complex64)
+    o = cap.opts(form=_lib.FORM_PLAIN, refine=_lib.REFINE_ALL)
+    assert cap.Capon().getCaponEx(z, P, w, None, x, 1e-3, 64, 4, 128, 3, x.shape[1], 0, o) == 0
+    e = errors(z, P, w, ref)
+    print(f"precise refined L64: P max {e['P'].max():.2e}, w max {e['w'].max():.2e}")
+    assert e["P"].max() <= 1e-6 and e["w"].max() <= 1e-5

@@ -270,3 +270,18 @@ def test_refinement_at_l32():
     # blocked path's z/P, not the L = 32 kernel's) decides for most pixels
     plain = o2["P"] != o1["P"]
     assert plain.mean() > 0.5
+
+
+def test_refinement_at_l16():
+    """L = 16 (config-0 shape): refinement in the fused path through the
+    16-lanes-per-pixel instantiation of the blocked path."""
+    from cos_gb300 import _lib, synth
+    c = synth.config0(seed=0)
+    x = np.ascontiguousarray(c["x"][:6])
+    ref = oracle.capon(x, c["d"], c["L"], c["K"], nthreads=6)
+    o1 = run(x, c["L"], c["K"], c["d"], want_w=True, refine=_lib.REFINE_ALL)
+    msg = check(o1, ref, "L16 refined")
+    eP = np.abs(o1["P"] - ref["P"]) / ref["P"]
+    ew = np.linalg.norm(o1["w"] - ref["w"], axis=-1) / np.linalg.norm(ref["w"], axis=-1)
+    assert eP.max() <= 1e-6 and ew.max() <= 1e-5, msg
+    check(run(x, c["L"], c["K"], c["d"], refine=_lib.REFINE_ADAPTIVE), ref, "L16 adaptive")
