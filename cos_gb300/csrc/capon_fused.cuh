@@ -120,11 +120,14 @@ struct Cfg {
     // the blocked per-pixel path of capon_fused_wide.cuh: always for L > 32;
     // at L <= 32 an instantiation of it serves the refinement modes
     static constexpr bool WIDE = WIDE_;
-    // float4 slots of a pixel group's shared area: the pivot-row buffers (and,
-    // wide, the first covariance row and the 1/d of factored rows), or the
-    // G x (G+1) exchange area of the w mode's back substitution
+    // float4 slots of a pixel group's shared area, the largest of: the
+    // pivot-row buffers (and, wide, the first covariance row and the 1/d of
+    // factored rows); the G x (G+1) exchange area of the back substitution;
+    // and, wide, the refinement's x0 (L complex) and its 8 x G partial sums
     static constexpr int AREA = WIDE ? WideArea<L, G>::Q : 2 * (L + 1);
-    static constexpr int RBQ = AREA > (G * (G + 1) + 1) / 2 ? AREA : (G * (G + 1) + 1) / 2;
+    static constexpr int XCH = (G * (G + 1) + 1) / 2;
+    static constexpr int RES = WIDE ? (L + 1) / 2 + 8 * G : 0;
+    static constexpr int RBQ = AREA > XCH ? (AREA > RES ? AREA : RES) : (XCH > RES ? XCH : RES);
     static_assert(L % G == 0 && 32 % G == 0, "G must divide L and 32");
     static_assert(WIDE || !RT_T, "a run-time window needs the L > 32 path");
 };

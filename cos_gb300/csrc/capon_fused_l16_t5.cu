@@ -27,7 +27,7 @@ const FusedCandidate kCand[] = {
     {"L16.G4.W8.N1.M32.T5", 16, 5, 32, launch_1, fused::smem_bytes<fused::Cfg<16, 4, 8, 1, 5, 32, false>>},
     {"L16.G4.W8.N1.sync.T5", 16, 5, 0, launch_2, fused::smem_bytes<fused::Cfg<16, 4, 8, 1, 5, 0, true>>},
     // the refinement modes (capon_fused_l16r.cu)
-    {"L16.G16.W8.refine", 16, 0, 0, fused_l16r_launch, fused_l16r_smem, fused_l16r_stash, true},
+    {"L16.G8.W8.refine", 16, 0, 0, fused_l16r_launch, fused_l16r_smem, fused_l16r_stash, true},
 };
 }  // namespace
 

@@ -27,7 +27,7 @@ const FusedCandidate kCand[] = {
     {"L32.G8.W8.N2.M64.T5", 32, 5, 64, launch_1, fused::smem_bytes<fused::Cfg<32, 8, 8, 2, 5, 64, false>>},
     {"L32.G8.W8.N2.sync.T5", 32, 5, 0, launch_2, fused::smem_bytes<fused::Cfg<32, 8, 8, 2, 5, 0, true>>},
     // the refinement modes (capon_fused_l32r.cu)
-    {"L32.G32.W12.refine", 32, 0, 0, fused_l32r_launch, fused_l32r_smem, fused_l32r_stash, true},
+    {"L32.G16.W12.refine", 32, 0, 0, fused_l32r_launch, fused_l32r_smem, fused_l32r_stash, true},
 };
 }  // namespace
 

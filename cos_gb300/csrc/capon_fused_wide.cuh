@@ -69,7 +69,8 @@ COS_DEV void static_for(F &&f)
     }
 }
 
-// shared area of one pixel group for the wide path (float4 units):
+// shared area of one pixel group for the wide path (float4 units; Cfg::RBQ
+// also covers the back substitution's exchange and the refinement's residual):
 //   [0, L+G)                   first covariance row, hi at float2 G + d, lo at L + 2G + d (-G < d < L)
 //   [L+G, L+G + 2(L+1))        two pivot-row buffers (the Schur steps use their first G slots)
 //   then L floats              1/d_p of the factored rows
@@ -139,6 +140,8 @@ COS_DEV void wide_pixel(const FrameDev &f, const float4 *xw, const int XS, const
     constexpr bool WMODE = MODE == FUSED_W || MODE == FUSED_REFINE;
     using WA = WideArea<L, G>;
     using WS = WideStash<L, G>;
+    static_assert(WA::Q <= C::RBQ && (G * (G + 1) + 1) / 2 <= C::RBQ && (L + 1) / 2 + 8 * G <= C::RBQ,
+                  "the pixel group's shared area holds every phase's layout");
     float2 *const r0h = (float2 *)area + G;
     float2 *const r0l = r0h + L + G;
     float4 *const pb = area + WA::PBQ;
@@ -518,7 +521,7 @@ COS_DEV void wide_pixel(const FrameDev &f, const float4 *xw, const int XS, const
             // high parts are exact, sums float-float; the residual itself is
             // assembled in FP64.
             float2 *const xs = (float2 *)area;         // x0, L entries
-            float4 *const red = area + (L + 1) / 2;    // 8 rows x G partial sums
+            float4 *const red = area + (L + 1) / 2;    // 8 rows x G partial sums (within Cfg::RBQ)
             __syncwarp();
 #pragma unroll
             for (int m = 0; m < NM; ++m) xs[m * G + r] = xv[m];
