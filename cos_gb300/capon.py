@@ -133,7 +133,8 @@ def getCaponCUDAPy(Xd, d, L, Navg, V, doFBAvg=False, verbose=False, want_R: bool
 
 
 def getCaponGPU(Xd, regCoef, L, Navg, V=None, doFBAvg=False, verbose=False, *, form=_lib.FORM_FUSED,
-                loading=_lib.LOAD_ELEMENT, want_w: bool = True, subspace=None, segment: int = 0):
+                loading=_lib.LOAD_ELEMENT, want_w: bool = True, subspace=None, segment: int = 0,
+                refine: int = _lib.REFINE_NONE):
     """getCaponCPy argument order on the GPU path: returns [z, P, w]
     (complex64 z, float32 P, complex64 w or None).  doFBAvg applies
     forward-backward averaging (the reference CPU path accepts the flag and
@@ -141,7 +142,8 @@ def getCaponGPU(Xd, regCoef, L, Navg, V=None, doFBAvg=False, verbose=False, *, f
     V, as in the reference GPU path, gives only the beam count Nb = V.shape[0]
     (the Butler matrix is used); `subspace` (complex [Nb][L]) is a caller-given
     subspace matrix with getCaponAllC.pyx:226-231, 365-370 semantics.
-    `segment` sets the build-up interval of FORM_SLIDING_INVERSE.
+    `segment` sets the build-up interval of FORM_SLIDING_INVERSE.  `refine`
+    (REFINE_ALL, REFINE_ADAPTIVE) adds the FP64-residual refinement step.
     Raises CaponError on a nonzero status."""
     Xd = np.ascontiguousarray(Xd, dtype=np.complex64)
     Nx, Ny, M = Xd.shape
@@ -154,14 +156,15 @@ def getCaponGPU(Xd, regCoef, L, Navg, V=None, doFBAvg=False, verbose=False, *, f
         Vs = np.ascontiguousarray(subspace, dtype=np.complex64)
         if Vs.ndim != 2 or Vs.shape[1] != L:
             raise ValueError("subspace must be [Nb][L]")
-        o = opts(form=form, loading=loading, fb=int(bool(doFBAvg)), segment=segment)
+        o = opts(form=form, loading=loading, fb=int(bool(doFBAvg)), segment=segment, refine=refine)
         check(lib.cos_capon_get_capon_subspace(_module_ctx().handle, _ptr(z), _ptr(P),
                                                _ptr(w) if w is not None else None, _ptr(Xd), _ptr(Vs),
                                                float(regCoef), L, Navg, M, Nx, Ny, int(Vs.shape[0]), C.byref(o)),
               "cos_capon_get_capon_subspace")
         return [z, P, w]
     check(_module_ctx().getCaponEx(z, P, w, None, Xd, float(regCoef), L, Navg, M, Nx, Ny, Nb,
-                                   opts(form=form, loading=loading, fb=int(bool(doFBAvg)), segment=segment)),
+                                   opts(form=form, loading=loading, fb=int(bool(doFBAvg)), segment=segment,
+                                        refine=refine)),
           "cos_capon_get_capon_ex")
     return [z, P, w]
 
