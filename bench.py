@@ -812,9 +812,10 @@ def run_profile_case(args) -> None:
                                                       device="cuda") if args.profile_w else None))
     ctx = capon.Context()
     for _ in range(args.warmup + args.steps):
-        capon.capon_frames(frames, ctx, capon.opts(form=args.profile_form))
+        capon.capon_frames(frames, ctx, capon.opts(form=args.profile_form, refine=args.profile_refine))
     torch.cuda.synchronize()
-    print(json.dumps({"profile_case": {"workload": wl, "Nx": args.profile_nx, "launches": args.warmup + args.steps}}))
+    print(json.dumps({"profile_case": {"workload": wl, "Nx": args.profile_nx, "refine": args.profile_refine,
+                                       "launches": args.warmup + args.steps}}))
 
 
 def main() -> None:
@@ -830,6 +831,7 @@ def main() -> None:
     ap.add_argument("--profile-form", type=int, default=0, help="form of the profiling case (COS_CAPON_FORM_*)")
     ap.add_argument("--profile-workload", default="config1", choices=["config1", "config2", "config3"])
     ap.add_argument("--profile-w", action="store_true", help="the profiling case also writes the weights w")
+    ap.add_argument("--profile-refine", type=int, default=0, help="the profiling case's opts.refine (COS_CAPON_REFINE_*)")
     ap.add_argument("--profile-nx", type=int, default=0,
                     help="profiling case: only the fused kernel, warmup+steps launches on Nx beams of the workload")
     args = ap.parse_args()
