@@ -285,3 +285,33 @@ def test_refinement_at_l16():
     ew = np.linalg.norm(o1["w"] - ref["w"], axis=-1) / np.linalg.norm(ref["w"], axis=-1)
     assert eP.max() <= 1e-6 and ew.max() <= 1e-5, msg
     check(run(x, c["L"], c["K"], c["d"], refine=_lib.REFINE_ADAPTIVE), ref, "L16 adaptive")
+
+
+def test_refinement_in_a_multi_frame_call_equals_single_calls():
+    """One call with an L=32 and an L=64 frame and refinement: the groups
+    share the context's stash one after the other; each frame's outputs equal
+    its own single-frame call bit for bit."""
+    import torch
+    from cos_gb300 import _lib, capon, synth
+    a = synth.config1(seed=4, Nx=2, Ny=90)["x"]
+    b, _ = config3_slice(Nx=2, Ny=90)
+    shapes = [(a, 32, 2, 0.01), (b, 64, 4, 1e-3)]
+    o = capon.opts(form=_lib.FORM_FUSED, refine=_lib.REFINE_ALL)
+    ctx = capon.Context()
+
+    def frame(x, L, K, d):
+        f = capon.DeviceFrame(x=torch.from_numpy(x).cuda(), L=L, K=K, d=d)
+        f.P = torch.empty((x.shape[0], x.shape[1] - 2 * K), dtype=torch.float32, device="cuda")
+        return f
+
+    singles = []
+    for sh in shapes:
+        f = frame(*sh)
+        capon.capon_frames([f], ctx, o)
+        singles.append(f)
+    both = [frame(*sh) for sh in shapes]
+    capon.capon_frames(both, ctx, o)
+    torch.cuda.synchronize()
+    for f, g in zip(both, singles):
+        assert np.array_equal(f.P.cpu().numpy(), g.P.cpu().numpy())
+        assert np.array_equal(f.z.cpu().numpy(), g.z.cpu().numpy())
