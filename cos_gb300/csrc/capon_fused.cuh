@@ -182,7 +182,8 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
     float2 *cs = (float2 *)(smem + S.off_c);
     float2 *cl = cs + (size_t)S.rows * L;
     float2 *gs = (float2 *)(smem + S.off_g);
-    // two pivot-row buffers per pixel group, alternating by Cholesky step
+    // each pixel group's shared area (Cfg::RBQ float4): the two pivot-row
+    // buffers, alternating by Cholesky step, and what else its phases keep
     float4 *rb = (float4 *)(smem + S.off_rb) + (size_t)(warp * PPW + gi) * C::RBQ;
     uint64_t *bar = (uint64_t *)(smem + S.off_bar);
 
@@ -288,35 +289,35 @@ fused_kernel(const __grid_constant__ FramesParam fp, long long total_units, unsi
                     w2 = w3;
                 }
             } else {
-            // three chunks per iteration: enough independent work to cover the
-            // load and TwoSum latencies, without the code growth of a full
-            // unroll (which slows the unrolled per-pixel phases that follow
-            // through the instruction cache)
+                // three chunks per iteration: enough independent work to cover the
+                // load and TwoSum latencies, without the code growth of a full
+                // unroll (which slows the unrolled per-pixel phases that follow
+                // through the instruction cache)
 #pragma unroll 3
-            for (int s0 = 0; s0 < Ns; s0 += 4) {
-                float2 P[4], Q[4];
+                for (int s0 = 0; s0 < Ns; s0 += 4) {
+                    float2 P[4], Q[4];
 #pragma unroll
-                for (int q = 0; q < 4; ++q) P[q] = Q[q] = make_float2(0.f, 0.f);
+                    for (int q = 0; q < 4; ++q) P[q] = Q[q] = make_float2(0.f, 0.f);
 #pragma unroll
-                for (int ss = 0; ss < 4; ++ss) {
-                    const int s = s0 + ss;
-                    if (s < Ns) {
-                        const float4 a = xr[s], w3 = xr[s + j0 + 3];
-                        const float4 c[4] = {w0, w1, w2, w3};
+                    for (int ss = 0; ss < 4; ++ss) {
+                        const int s = s0 + ss;
+                        if (s < Ns) {
+                            const float4 a = xr[s], w3 = xr[s + j0 + 3];
+                            const float4 c[4] = {w0, w1, w2, w3};
 #pragma unroll
-                        for (int q = 0; q < 4; ++q) {
-                            // a * conj(c): P += (ar, ai).(cr, ci), Q += (ai, -ar).(cr, ci)
-                            P[q] = ffma2(make_float2(a.x, a.y), make_float2(c[q].x, c[q].y), P[q]);
-                            Q[q] = ffma2(make_float2(a.z, a.w), make_float2(c[q].x, c[q].y), Q[q]);
+                            for (int q = 0; q < 4; ++q) {
+                                // a * conj(c): P += (ar, ai).(cr, ci), Q += (ai, -ar).(cr, ci)
+                                P[q] = ffma2(make_float2(a.x, a.y), make_float2(c[q].x, c[q].y), P[q]);
+                                Q[q] = ffma2(make_float2(a.z, a.w), make_float2(c[q].x, c[q].y), Q[q]);
+                            }
+                            w0 = w1;
+                            w1 = w2;
+                            w2 = w3;
                         }
-                        w0 = w1;
-                        w1 = w2;
-                        w2 = w3;
                     }
-                }
 #pragma unroll
-                for (int q = 0; q < 4; ++q) two_sum_acc(hi[q], lo[q], make_float2(P[q].x + P[q].y, Q[q].x + Q[q].y));
-            }
+                    for (int q = 0; q < 4; ++q) two_sum_acc(hi[q], lo[q], make_float2(P[q].x + P[q].y, Q[q].x + Q[q].y));
+                }
             }
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
