@@ -315,3 +315,36 @@ def test_refinement_in_a_multi_frame_call_equals_single_calls():
     for f, g in zip(both, singles):
         assert np.array_equal(f.P.cpu().numpy(), g.P.cpu().numpy())
         assert np.array_equal(f.z.cpu().numpy(), g.z.cpu().numpy())
+
+
+def _sweep_cases(n, seed):
+    rng = np.random.default_rng(seed)
+    cases = []
+    for _ in range(n):
+        L = int(rng.choice([16, 32, 48, 64]))
+        K = int(rng.integers(0, 5 if L > 32 else 3))
+        M = int(rng.integers(L + 16, min(L + 80, 150) + 1))
+        Ny = int(rng.integers(2 * K + 1, 90))
+        Nx = int(rng.integers(1, 4))
+        refine = int(rng.integers(0, 3))
+        loading = int(rng.choice([0, 2]))
+        cases.append((L, K, M, Ny, Nx, refine, loading, int(rng.integers(1 << 30))))
+    return cases
+
+
+@pytest.mark.parametrize("L,K,M,Ny,Nx,refine,loading,seed", _sweep_cases(10, 2024))
+def test_random_shapes(L, K, M, Ny, Nx, refine, loading, seed):
+    """Seeded random shapes through the fused path: L = 48 and 64 (z/P and
+    refinement) and the refinement modes at L = 16 and 32; odd and even M,
+    short beams, both loading conventions."""
+    if L <= 32 and refine == 0:
+        refine = 1   # the L <= 32 kernels' own z/P is covered elsewhere
+    if (M - L + 1) * (2 * K + 1) < 2 * L and refine == 0:
+        refine = 1   # fewer snapshots than 2L: an ill-conditioned R, FP32-limited
+    rng = np.random.default_rng(seed)
+    x = (rng.standard_normal((Nx, Ny, M)) + 1j * rng.standard_normal((Nx, Ny, M))).astype(np.complex64)
+    x[:, Ny // 2] *= 8.0   # one strong range row
+    d = 0.05 if loading == 2 else 0.01
+    ref = oracle.capon(x, d, L, K, want_w=False, absolute=loading == 2, fp32_scalars=loading != 2)
+    o = run(x, L, K, d, loading=loading, refine=refine)
+    check(o, ref, f"L{L} K{K} M{M} Ny{Ny} Nx{Nx} refine{refine} load{loading}")
