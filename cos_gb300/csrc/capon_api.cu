@@ -169,9 +169,13 @@ static bool use_fused(const FrameDev &f, const cos_capon_opts &o)
     if (o.refine && !refine_in_fused(f, o)) return false;
     const FusedCandidate *c = nullptr;
     const int n = candidates(f.L, f.K, o.form, &c);
-    for (int i = 0; i < n; ++i)
-        if (cand_fits(c[i], f, o.refine != 0)) return true;
-    return false;
+    bool refine_fit = false, basic_fit = false;
+    for (int i = 0; i < n; ++i) {
+        refine_fit |= cand_fits(c[i], f, true);
+        basic_fit |= cand_fits(c[i], f, false);
+    }
+    // with refinement, R (when asked for) still comes from a z/P-w-R candidate
+    return o.refine ? refine_fit && (!f.R || basic_fit) : basic_fit;
 }
 
 // Autotuner: the first launch of an (L, K, M, mode) shape on a context times
